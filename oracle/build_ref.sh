@@ -1,0 +1,54 @@
+#!/usr/bin/env bash
+# Builds the reference's own CPU path (ShugangZhang/LQT1) from its sources
+# where they lie, into oracle/_ref/ (git-ignored).  TEST INFRASTRUCTURE ONLY.
+#
+# Nothing is copied: scenario variants are produced by streaming the
+# reference's files through `sed` into the compiler.  Every patch is listed
+# here and is limited to the scenario macros, the LQT1 factor, the stimulus
+# duration, and (for the update() harness only) `private:` -> `public:` so that
+# the harness can read and set the 40 states.
+#
+#   model_single_cell, model_oned          unmodified drivers, Makefile:20-35 flags
+#   model_oned_cfg1                        OneD.cc + TPORd.cc with CON->LQT1, ISO1
+#                                          off, GKs x0.5 (TPORd.cc:706) and a 2 ms
+#                                          stimulus (OneD.cc:80)
+# (TPORd.cc has CRLF line ends, hence the optional \r in the patterns.)
+#   libtpord_ref_{default,baseline,lqt1,lqt1half,suprep}.so
+#                                          TPORd.cc + oracle/ref_harness.inc
+#
+# Usage: oracle/build_ref.sh [REFERENCE_DIR]
+set -euo pipefail
+REF=${1:-${LQT_REFERENCE:-/root/reference}}
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT="$HERE/_ref"
+[ -f "$REF/SingleCell/TPORd.cc" ] || { echo "reference not found at $REF" >&2; exit 2; }
+mkdir -p "$OUT"
+CXX=${CXX:-g++}
+TPORD="$REF/SingleCell/TPORd.cc"
+
+# 1. unmodified drivers (Makefile:30-35 recipes; target SingleCell is shadowed
+#    by the SingleCell/ directory in the reference's make, so it is built here).
+$CXX -w -O3 -o "$OUT/model_single_cell" "$REF/SingleCell/Cell.cc" "$TPORD" "$REF/SingleCell.cc" &
+$CXX -w -O3 -fopenmp -o "$OUT/model_oned" "$REF/SingleCell/Cell.cc" "$TPORD" "$REF/OneD.cc" &
+
+# 2. scenario variant of the 1D driver for the 1D strand workload.
+SCEN_LQT1HALF=(-e 's|^#define CON\r\?$|#define LQT1|' -e 's|^#define ISO1\r\?$|// ISO1 off|' \
+               -e 's|GKs = 0.05\*GKs;|GKs = 0.5*GKs;|')
+{ sed "${SCEN_LQT1HALF[@]}" "$TPORD"
+  sed -e 's|^#include "SingleCell/TPORd.cc"|// TPORd streamed above|' \
+      -e 's|double stimDuration = 1.0;|double stimDuration = 2.0;|' "$REF/OneD.cc"; } |
+  $CXX -w -O3 -fopenmp -x c++ -I"$REF/SingleCell" -o "$OUT/model_oned_cfg1" - &
+
+# 3. update() harness, one library per scenario.
+harness() {
+  local name=$1; shift
+  { sed -e 's|^private:\r\?$|public:|' "$@" "$TPORD"; cat "$HERE/ref_harness.inc"; } |
+    $CXX -w -O3 -fPIC -shared -fopenmp -x c++ -I"$REF/SingleCell" -o "$OUT/libtpord_ref_$name.so" -
+}
+harness default -e 's|^//__none__||' &
+harness baseline -e 's|^#define CON\r\?$|#define BASELINE|' -e 's|^#define ISO1\r\?$|// ISO1 off|' &
+harness lqt1 -e 's|^#define CON\r\?$|#define LQT1|' -e 's|^#define ISO1\r\?$|// ISO1 off|' &
+harness lqt1half "${SCEN_LQT1HALF[@]}" &
+harness suprep -e 's|^// #define SUPREP\r\?$|#define SUPREP|' &
+wait
+echo "reference built into $OUT"
