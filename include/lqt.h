@@ -132,6 +132,72 @@ int lqt_cells_get_v(lqt_cells *c, double *v_host);
 int lqt_cells_get_dvdt(lqt_cells *c, double *dvdt_host);
 
 /* ======================================================================== *
+ *  Batches of independent instances: single cells and 1D strands, run to
+ *  completion in one persistent launch.  Replaces the OneD.cc:100-436 strand
+ *  loop (stimulus to the first cells, mirrored-end diffusion
+ *  dVgap = dD/dx dV/dx + D d2V/dx2, update) and the SingleCell.cc:95-109 loop,
+ *  for many instances with their own parameters at once.
+ * ======================================================================== */
+typedef struct lqt_batch lqt_batch;
+
+typedef struct lqt_instance {
+    int32_t ncells;            /* 1 = single cell; > 1 = strand (OneD.cc:100) */
+    int32_t n_stim;            /* cells [0, n_stim) receive S1 (3 in OneD.cc:340) */
+    int32_t model;             /* index into the models array */
+    int32_t record;            /* 1 = record V every rec_every steps; strands also
+                                  record the pseudo-ECG at ecg_x0 */
+    double dx;                 /* mm (0.15, OneD.cc:47) */
+    double bcl;                /* ms */
+    double s1_start;           /* ms into each cycle */
+    double s1_duration;        /* ms */
+    double s1_strength;        /* pA/pF */
+    int32_t s1_beats;          /* stimulated cycles; 0 = every cycle */
+    int32_t reserved0;
+    double t_stop;             /* steps run while time <= t_stop (OneD.cc:317) */
+    double ecg_x0;             /* electrode, mm from cell 0 (35 in plot1DECG_compare.py:83) */
+    double act_threshold;      /* mV (-30, OneD.cc:422) */
+} lqt_instance;
+
+typedef struct lqt_batch_params {
+    double dt;                 /* ms */
+    double v0;                 /* initial V (-87.5, SingleCell/TPORd.cc:144) */
+    int32_t precision;         /* LQT_FP64 or LQT_MIXED */
+    int32_t max_beats;         /* detector slots per cell */
+    int64_t rec_every;         /* steps between V records (10 in OneD.cc:402) */
+    int32_t threads;           /* CTA width; 0 = autotuned */
+    int32_t ctas;              /* persistent CTAs; 0 = autotuned */
+    void *stream;              /* cudaStream_t or NULL */
+} lqt_batch_params;
+
+/* cell_types: all cells, instance by instance (sum of ncells).
+ * coeff: per-cell diffusion coefficient D (mm^2/ms) or NULL = 0.154
+ * (OneD.cc:68); dD/dx is formed as OneD.cc:123-131 does. */
+int lqt_batch_create(const lqt_batch_params *params, int32_t ninst,
+                     const lqt_instance *inst, const uint8_t *cell_types_host,
+                     const double *coeff_host, int32_t nmodels,
+                     const lqt_model *models, lqt_batch **out);
+void lqt_batch_destroy(lqt_batch *b);
+int64_t lqt_batch_num_cells(const lqt_batch *b);
+/* Run every instance to its t_stop (one persistent launch). */
+int lqt_batch_run(lqt_batch *b);
+/* Per cell (input order) and beat: activation time, APD90, max |dV/dt| of the
+ * upstroke ([cells][max_beats], -1 = none), EAD flag and beats seen. */
+int lqt_batch_get_detect(lqt_batch *b, float *t_act, float *apd90,
+                         float *dvdt_max, uint8_t *ead, int32_t *nbeats);
+/* Recorded V of instance i ([nrec][ncells]), record times and pseudo-ECG. */
+int lqt_batch_get_record(lqt_batch *b, int32_t inst, float *v, double *t,
+                         double *ecg, int64_t cap, int64_t *nrec);
+int lqt_batch_get_state(lqt_batch *b, double *state_host);
+int lqt_batch_set_state(lqt_batch *b, const double *state_host);
+/* Device time of the last run, ms (CUDA events on the batch stream). */
+double lqt_batch_last_run_ms(const lqt_batch *b);
+/* Blow-up counter of the last run (voxel-steps with NaN or V out of range). */
+int64_t lqt_batch_num_bad(lqt_batch *b);
+
+/* Last error message of the calling thread ("" if none). */
+const char *lqt_last_error(void);
+
+/* ======================================================================== *
  *  Tissue simulation: 1D strand, 2D sheet or 3D volume with diffusion.
  *  Replaces the OneD.cc:317-436 loop (1D) and the GPU3D.cu / new_11.cu
  *  kernel chain calc_du -> init_Istim -> set_Istim -> Itot -> new_u_v.
@@ -171,7 +237,8 @@ typedef struct lqt_sim_params {
     int32_t detect;            /* 1 = on-device activation / APD90 / EAD detectors */
     lqt_model model;
     double act_threshold;      /* mV, activation crossing (-30, OneD.cc:422) */
-    double vmin_ok, vmax_ok;   /* blow-up detector range (GPU3D.cu:1805-1817: -90/200 warn) */
+    double vmin_ok, vmax_ok;   /* blow-up detector range (GPU3D.cu:1805-1817 warns below
+                                  -90 / above 200); vmin_ok >= vmax_ok = NaN check only */
     void *stream;              /* cudaStream_t or NULL */
 } lqt_sim_params;
 
@@ -213,6 +280,12 @@ int lqt_sim_get_ecg(lqt_sim *s, int64_t max_samples, double *phi_host,
 int lqt_sim_get_detect(lqt_sim *s, float *t_act_host, float *apd90_host,
                        uint8_t *ead_host);
 
+/* Mirror-boundary map (GPU3D.cu:1487-1604): the empty grid voxels next to
+ * tissue and, for each, the grid index of the tissue voxel whose V it holds.
+ * Call with dst = src = NULL to get the count. */
+int lqt_sim_boundary(const lqt_sim *s, int64_t *dst_host, int64_t *src_host,
+                     int64_t *n);
+
 /* Blow-up detector: count of voxels with NaN or V outside [vmin_ok, vmax_ok]
  * since the last call (GPU3D.cu:1796-1829 does this scan on the host). */
 int lqt_sim_check(lqt_sim *s, int64_t *n_bad);
@@ -220,6 +293,55 @@ int lqt_sim_check(lqt_sim *s, int64_t *n_bad);
 /* Binary checkpoint: header + version + per-state arrays. */
 int lqt_sim_checkpoint(lqt_sim *s, const char *path);
 int lqt_sim_restore(lqt_sim *s, const char *path);
+
+/* ======================================================================== *
+ *  Synthetic geometries (seeded).  The reference reads its geometry from
+ *  files that are not distributed (wholeventriclewithfibervector.txt,
+ *  157layerwithfibervector.txt, GPU3D.cu:1276, new_11.cu:1296); these
+ *  generators produce grids in the same layout (x-major, z fastest).
+ * ======================================================================== */
+
+/* 2D sheet of nx*ny tissue voxels in a grid of (nx+2)*(ny+2) (one empty
+ * voxel on each side; all arrays have the grid's size): types in bands along
+ * x (frac_endo endo, frac_mid M, rest epi); s1_mask = first s1_cols tissue
+ * columns; s2_mask = tissue quadrant x < nx/2, y < ny/2.  Masks may be NULL. */
+int lqt_geom_sheet(int32_t nx, int32_t ny, double frac_endo, double frac_mid,
+                   int32_t s1_cols, uint8_t *types, uint8_t *s1_mask,
+                   uint8_t *s2_mask);
+
+/* Truncated prolate-ellipsoid shell (all lengths mm): outer semi-axes a_out
+ * (x, y) and c_out (z), wall thickness `wall`, axis at (cx, cy), base plane
+ * z = z_base (tissue below it), apex at z_base - c_out.  Transmural depth
+ * e in [0,1] (endo -> epi): endo for e < endo_frac, epi for e >= 1 - epi_frac;
+ * between them M cells inside a seeded spherical island of island_radius in
+ * the free wall (centre returned in island_out[3]), endo/epi outside it (as
+ * GPU3D.cu:1440-1461 cancels M cells outside its island).  Fibre angle
+ * linear in e from alpha_endo_deg to alpha_epi_deg, measured from the
+ * circumferential direction towards the meridian.  s1_mask: tissue within
+ * stim_radius of the apex. */
+typedef struct lqt_ventricle_spec {
+    int32_t nx, ny, nz;
+    int32_t reserved0;
+    double dx;
+    double a_out, c_out, wall;
+    double cx, cy, z_base;
+    double endo_frac, epi_frac;
+    double island_radius;
+    double alpha_endo_deg, alpha_epi_deg;
+    double stim_radius;
+    uint64_t seed;
+} lqt_ventricle_spec;
+
+int lqt_geom_ventricle(const lqt_ventricle_spec *spec, uint8_t *types,
+                       float *fibre, uint8_t *s1_mask, double *island_out);
+
+/* Host-only tissue numbering and mirror-boundary map of a grid (what
+ * lqt_sim_create builds; GPU3D.cu:1307-1333, 1487-1604; new_11.cu:1535-1640).
+ * tissue_of[nx*ny*nz]: tissue index or -1.  bnd_dst/bnd_src: boundary voxel
+ * and its mirror source (grid indices); NULL to query *nbnd first. */
+int lqt_geom_mirror_map(int32_t nx, int32_t ny, int32_t nz,
+                        const uint8_t *types, int32_t *tissue_of,
+                        int64_t *bnd_dst, int64_t *bnd_src, int64_t *nbnd);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,453 @@
+// api_batch.cu -- lqt_batch_*: uneven batches of single cells and strands in
+// one persistent launch (k_batch.cu).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "api_common.h"
+
+using namespace lqt;
+
+struct lqt_batch {
+    lqt_batch_params p{};
+    int64_t ncells = 0, ld = 0;
+    int32_t ninst = 0;
+    int threads = 128, ctas = 152;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    float last_ms = 0.f;
+    DevMem mem;
+    std::vector<int64_t> perm;          // internal cell -> input cell
+    std::vector<lqt_instance> inst;
+    std::vector<int64_t> inst_cell0;    // input order: first cell of each instance
+    std::vector<int64_t> inst_internal0;// internal first cell of each instance
+    std::vector<int32_t> rec_slot;      // per instance
+    std::vector<int64_t> inst_nsteps;
+    int64_t rec_cap = 0;
+    int32_t rec_width = 0;
+    // device
+    void *v = nullptr, *gate = nullptr;
+    double *conc = nullptr, *aos = nullptr;
+    uint8_t *ctype = nullptr;
+    double *coeff = nullptr, *dcoeff = nullptr;
+    int32_t *seg_of = nullptr;
+    Seg *segs = nullptr;
+    Item *items = nullptr;
+    int32_t nitems = 0;
+    Win *win = nullptr;
+    ModelK *models = nullptr;
+    int *queue = nullptr;
+    unsigned long long *nbad = nullptr;
+    float *rec_v = nullptr;
+    double *rec_t = nullptr, *ecg = nullptr;
+    float *det_t_act = nullptr, *det_apd90 = nullptr, *det_dvdt = nullptr;
+    uint8_t *det_ead = nullptr;
+    int32_t *det_beats = nullptr;
+
+    ~lqt_batch()
+    {
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+    }
+    template <typename R> BatchDev<R> dev() const
+    {
+        BatchDev<R> b{};
+        b.s = SoA<R>{(R *)v, conc, (R *)gate, ld};
+        b.ctype = ctype;
+        b.coeff = coeff;
+        b.dcoeff = dcoeff;
+        b.seg_of = seg_of;
+        b.segs = segs;
+        b.items = items;
+        b.nitems = nitems;
+        b.max_beats = p.max_beats;
+        b.win = win;
+        b.models = models;
+        b.queue = queue;
+        b.nbad = nbad;
+        b.vmin_ok = -200.0;
+        b.vmax_ok = 200.0;
+        b.rec_every = p.rec_every;
+        b.rec_cap = rec_cap;
+        b.rec_width = rec_width;
+        b.rec_v = rec_v;
+        b.rec_t = rec_t;
+        b.ecg = ecg;
+        b.det_t_act = det_t_act;
+        b.det_apd90 = det_apd90;
+        b.det_dvdt = det_dvdt;
+        b.det_ead = det_ead;
+        b.det_beats = det_beats;
+        return b;
+    }
+};
+
+static int upload(void *dst, const void *src, size_t bytes, cudaStream_t st)
+{
+    if (bytes == 0) return LQT_OK;
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+    return LQT_OK;
+}
+
+extern "C" {
+
+int lqt_batch_create(const lqt_batch_params *params, int32_t ninst, const lqt_instance *inst,
+                     const uint8_t *cell_types_host, const double *coeff_host, int32_t nmodels,
+                     const lqt_model *models, lqt_batch **out)
+{
+    if (!out) return fail(LQT_ERR_INVALID, "lqt_batch_create: out is NULL");
+    *out = nullptr;
+    if (!params || ninst <= 0 || !inst || !cell_types_host || nmodels <= 0 || !models)
+        return fail(LQT_ERR_INVALID, "lqt_batch_create: NULL argument or empty batch");
+    const lqt_batch_params &p = *params;
+    if (!(p.dt > 0) || !std::isfinite(p.dt)) return fail(LQT_ERR_INVALID, "lqt_batch_create: dt must be > 0");
+    if (p.precision != LQT_FP64 && p.precision != LQT_MIXED) return fail(LQT_ERR_INVALID, "lqt_batch_create: precision");
+    if (p.max_beats < 0 || p.max_beats > 4096) return fail(LQT_ERR_INVALID, "lqt_batch_create: max_beats");
+    if (p.rec_every <= 0) return fail(LQT_ERR_INVALID, "lqt_batch_create: rec_every must be > 0");
+    for (int i = 0; i < nmodels; ++i) {
+        int rc = check_model(models[i]);
+        if (rc) return rc;
+    }
+    int max_strand = 1;
+    int64_t ncells = 0;
+    double t_max = 0;
+    for (int i = 0; i < ninst; ++i) {
+        const lqt_instance &q = inst[i];
+        if (q.ncells < 1 || q.ncells > 512 || q.model < 0 || q.model >= nmodels || q.n_stim < 0 ||
+            !(q.t_stop >= 0) || !std::isfinite(q.t_stop) || !(q.bcl > 0) || q.s1_duration < 0 || q.s1_beats < 0 ||
+            (q.ncells > 1 && !(q.dx > 0)) || q.t_stop > 1e7)
+            return fail(LQT_ERR_INVALID, "lqt_batch_create: instance " + std::to_string(i) +
+                                             " invalid (ncells 1..512, model index, bcl > 0, t_stop, dx > 0)");
+        max_strand = std::max(max_strand, (int)q.ncells);
+        ncells += q.ncells;
+        t_max = std::max(t_max, q.t_stop);
+    }
+    for (int64_t i = 0; i < ncells; ++i)
+        if (cell_types_host[i] > LQT_MCELL) return fail(LQT_ERR_INVALID, "lqt_batch_create: cell type out of range");
+
+    auto *b = new lqt_batch();
+    b->p = p;
+    b->ninst = ninst;
+    b->ncells = ncells;
+    b->ld = pad128(ncells);
+    b->stream = (cudaStream_t)p.stream;
+    b->inst.assign(inst, inst + ninst);
+    b->threads = p.threads > 0 ? p.threads : (max_strand <= 128 ? 128 : (max_strand <= 256 ? 256 : 512));
+    if (b->threads != 128 && b->threads != 256 && b->threads != 512) {
+        delete b;
+        return fail(LQT_ERR_INVALID, "lqt_batch_create: threads must be 128, 256 or 512");
+    }
+    if (max_strand > b->threads) {
+        delete b;
+        return fail(LQT_ERR_INVALID, "lqt_batch_create: a strand is longer than the CTA width");
+    }
+
+    // time axis and per-instance step counts / windows
+    std::vector<double> times;
+    time_axis(p.dt, t_max, times);
+    b->inst_nsteps.resize(ninst);
+    std::vector<std::vector<Win>> wins(ninst);
+    for (int i = 0; i < ninst; ++i) {
+        const lqt_instance &q = inst[i];
+        int64_t ns = std::upper_bound(times.begin(), times.end(), q.t_stop) - times.begin();
+        b->inst_nsteps[i] = ns;
+        stim_windows(times, ns, p.dt, q.bcl, q.s1_start, q.s1_duration, q.s1_beats, wins[i]);
+    }
+
+    // items: strands alone, single cells packed by step count; largest first
+    b->inst_cell0.resize(ninst);
+    for (int i = 0, c0 = 0; i < ninst; ++i) {
+        b->inst_cell0[i] = c0;
+        c0 += inst[i].ncells;
+    }
+    std::vector<int> order(ninst);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+        const int64_t wa = b->inst_nsteps[a] * ((inst[a].ncells + 31) / 32);
+        const int64_t wc = b->inst_nsteps[c] * ((inst[c].ncells + 31) / 32);
+        if (inst[a].ncells > 1 || inst[c].ncells > 1) return wa > wc;
+        return b->inst_nsteps[a] > b->inst_nsteps[c];
+    });
+    std::vector<Item> items;
+    std::vector<Seg> segs(ninst);
+    std::vector<Win> allwin;
+    b->inst_internal0.assign(ninst, 0);
+    b->perm.resize(ncells);
+    b->rec_slot.assign(ninst, -1);
+    int32_t nrec_slots = 0;
+    int64_t next_cell = 0;
+    Item cur{};
+    cur.ncells = 0;
+    auto flush = [&]() {
+        if (cur.ncells > 0) items.push_back(cur);
+        cur = Item{};
+        cur.ncells = 0;
+    };
+    for (int oi : order) {
+        const lqt_instance &q = inst[oi];
+        const bool single = q.ncells == 1;
+        if (!single || cur.ncells + 1 > b->threads) flush();
+        if (cur.ncells == 0) {
+            cur.cell0 = next_cell;
+            cur.nsteps = 0;
+            cur.ecg_seg = -1;
+        }
+        Seg s{};
+        s.cell0 = next_cell;
+        s.nsteps = b->inst_nsteps[oi];
+        s.n = q.ncells;
+        s.n_stim = q.n_stim;
+        s.model = q.model;
+        s.win0 = (int32_t)allwin.size();
+        s.nwin = (int32_t)wins[oi].size();
+        allwin.insert(allwin.end(), wins[oi].begin(), wins[oi].end());
+        s.dx = q.dx;
+        s.stim = q.s1_strength;
+        s.ecg_x0 = q.ecg_x0;
+        s.act_thr = (float)q.act_threshold;
+        s.rec_slot = -1;
+        if (q.record) {
+            s.rec_slot = nrec_slots++;
+            b->rec_slot[oi] = s.rec_slot;
+            b->rec_width = std::max(b->rec_width, (int32_t)q.ncells);
+            if (!single) cur.ecg_seg = oi;
+        }
+        segs[oi] = s;
+        b->inst_internal0[oi] = next_cell;
+        for (int j = 0; j < q.ncells; ++j) b->perm[next_cell + j] = b->inst_cell0[oi] + j;
+        next_cell += q.ncells;
+        cur.ncells += q.ncells;
+        cur.nsteps = std::max(cur.nsteps, s.nsteps);
+        if (!single) flush();
+    }
+    flush();
+    b->nitems = (int32_t)items.size();
+    // segments are indexed by input instance; cell -> segment map (internal order)
+    std::vector<int32_t> seg_of(ncells);
+    for (int i = 0; i < ninst; ++i)
+        for (int j = 0; j < inst[i].ncells; ++j) seg_of[b->inst_internal0[i] + j] = i;
+    int64_t max_ns = 0;
+    for (auto ns : b->inst_nsteps) max_ns = std::max(max_ns, ns);
+    b->rec_cap = nrec_slots ? (max_ns + p.rec_every - 1) / p.rec_every : 0;
+
+    // per-cell inputs in internal order; dD/dx per strand as OneD.cc:123-131
+    std::vector<uint8_t> ct(ncells);
+    std::vector<double> co(ncells), dco(ncells);
+    for (int i = 0; i < ninst; ++i) {
+        const int n = inst[i].ncells;
+        const int64_t in0 = b->inst_cell0[i], it0 = b->inst_internal0[i];
+        for (int j = 0; j < n; ++j) {
+            ct[it0 + j] = cell_types_host[in0 + j];
+            co[it0 + j] = coeff_host ? coeff_host[in0 + j] : 0.154;
+        }
+        for (int j = 0; j < n; ++j) {
+            const double *cc = &co[it0];
+            double dd;
+            if (n == 1) dd = 0.0;
+            else if (j == 0) dd = (cc[j + 1] - cc[j]) / inst[i].dx;
+            else if (j == n - 1) dd = (cc[j] - cc[j - 1]) / inst[i].dx;
+            else dd = (cc[j + 1] - cc[j - 1]) / (2.0 * inst[i].dx);
+            dco[it0 + j] = dd;
+        }
+    }
+    std::vector<ModelK> mk(nmodels);
+    for (int i = 0; i < nmodels; ++i) mk[i] = make_modelk(models[i]);
+    std::vector<double> init((size_t)ncells * 40);
+    for (int64_t i = 0; i < ncells; ++i) initial_state(p.v0, &init[i * 40]);
+
+    const size_t rsz = p.precision == LQT_FP64 ? 8 : 4;
+    const int64_t ld = b->ld, nb = (int64_t)p.max_beats;
+    int rc = 0;
+    rc |= b->mem.alloc(&b->v, ld * rsz);
+    rc |= b->mem.alloc(&b->gate, ld * rsz * kNGate);
+    rc |= b->mem.alloc((void **)&b->conc, ld * 8 * kNConc);
+    rc |= b->mem.alloc((void **)&b->aos, ncells * 320);
+    rc |= b->mem.alloc((void **)&b->ctype, ncells);
+    rc |= b->mem.alloc((void **)&b->coeff, ncells * 8);
+    rc |= b->mem.alloc((void **)&b->dcoeff, ncells * 8);
+    rc |= b->mem.alloc((void **)&b->seg_of, ncells * 4);
+    rc |= b->mem.alloc((void **)&b->segs, ninst * sizeof(Seg));
+    rc |= b->mem.alloc((void **)&b->items, items.size() * sizeof(Item));
+    rc |= b->mem.alloc((void **)&b->win, allwin.size() * sizeof(Win));
+    rc |= b->mem.alloc((void **)&b->models, nmodels * sizeof(ModelK));
+    rc |= b->mem.alloc((void **)&b->queue, 16);
+    rc |= b->mem.alloc((void **)&b->nbad, 16);
+    if (nrec_slots) {
+        rc |= b->mem.alloc((void **)&b->rec_v, (size_t)nrec_slots * b->rec_cap * b->rec_width * 4);
+        rc |= b->mem.alloc((void **)&b->rec_t, (size_t)nrec_slots * b->rec_cap * 8);
+        rc |= b->mem.alloc((void **)&b->ecg, (size_t)nrec_slots * b->rec_cap * 8);
+    }
+    if (nb > 0) {
+        rc |= b->mem.alloc((void **)&b->det_t_act, ncells * nb * 4);
+        rc |= b->mem.alloc((void **)&b->det_apd90, ncells * nb * 4);
+        rc |= b->mem.alloc((void **)&b->det_dvdt, ncells * nb * 4);
+        rc |= b->mem.alloc((void **)&b->det_ead, ncells);
+        rc |= b->mem.alloc((void **)&b->det_beats, ncells * 4);
+    }
+    if (rc) {
+        std::string m = g_err;
+        delete b;
+        return fail(LQT_ERR_NOMEM, "lqt_batch_create: " + m);
+    }
+    std::vector<double> init_int((size_t)ncells * 40);
+    for (int64_t i = 0; i < ncells; ++i) std::memcpy(&init_int[i * 40], &init[b->perm[i] * 40], 320);
+    cudaStream_t st = b->stream;
+    rc = upload(b->ctype, ct.data(), ncells, st) | upload(b->coeff, co.data(), ncells * 8, st) |
+         upload(b->dcoeff, dco.data(), ncells * 8, st) | upload(b->seg_of, seg_of.data(), ncells * 4, st) |
+         upload(b->segs, segs.data(), ninst * sizeof(Seg), st) |
+         upload(b->items, items.data(), items.size() * sizeof(Item), st) |
+         upload(b->win, allwin.data(), allwin.size() * sizeof(Win), st) |
+         upload(b->models, mk.data(), nmodels * sizeof(ModelK), st) |
+         upload(b->aos, init_int.data(), ncells * 320, st);
+    if (rc) {
+        std::string m = g_err;
+        delete b;
+        return fail(LQT_ERR_CUDA, m);
+    }
+    cudaError_t e = p.precision == LQT_FP64
+                        ? launch_pack<double>(b->aos, SoA<double>{(double *)b->v, b->conc, (double *)b->gate, ld}, ncells, st)
+                        : launch_pack<float>(b->aos, SoA<float>{(float *)b->v, b->conc, (float *)b->gate, ld}, ncells, st);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        delete b;
+        return fail(LQT_ERR_CUDA, std::string("lqt_batch_create: ") + cudaGetErrorString(e));
+    }
+    int dev = 0, nsm = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int per_sm = p.precision == LQT_FP64 ? batch_max_ctas_per_sm<double>(b->threads)
+                                               : batch_max_ctas_per_sm<float>(b->threads);
+    b->ctas = p.ctas > 0 ? p.ctas : std::max(1, std::min(b->nitems, nsm * std::max(1, per_sm)));
+    *out = b;
+    return LQT_OK;
+}
+
+void lqt_batch_destroy(lqt_batch *b) { delete b; }
+
+int64_t lqt_batch_num_cells(const lqt_batch *b) { return b ? b->ncells : -1; }
+
+int lqt_batch_run(lqt_batch *b)
+{
+    if (!b) return fail(LQT_ERR_INVALID, "lqt_batch_run: NULL handle");
+    cudaStream_t st = b->stream;
+    CK(cudaMemsetAsync(b->queue, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(b->nbad, 0, sizeof(unsigned long long), st));
+    if (b->p.max_beats > 0) {
+        const int64_t nb = b->ncells * b->p.max_beats;
+        CK(cudaMemsetAsync(b->det_t_act, 0xff, nb * 4, st));   // 0xffffffff = NaN -> reported as -1
+        CK(cudaMemsetAsync(b->det_apd90, 0xff, nb * 4, st));
+        CK(cudaMemsetAsync(b->det_dvdt, 0xff, nb * 4, st));
+        CK(cudaMemsetAsync(b->det_ead, 0, b->ncells, st));
+        CK(cudaMemsetAsync(b->det_beats, 0, b->ncells * 4, st));
+    }
+    CK(cudaEventRecord(b->ev0, st));
+    CK(b->p.precision == LQT_FP64 ? launch_batch<double>(b->dev<double>(), make_stepk(b->p.dt), b->threads, b->ctas, st)
+                                  : launch_batch<float>(b->dev<float>(), make_stepk(b->p.dt), b->threads, b->ctas, st));
+    CK(cudaEventRecord(b->ev1, st));
+    CK(cudaEventSynchronize(b->ev1));
+    CK(cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1));
+    return LQT_OK;
+}
+
+double lqt_batch_last_run_ms(const lqt_batch *b) { return b ? b->last_ms : -1.0; }
+
+int64_t lqt_batch_num_bad(lqt_batch *b)
+{
+    if (!b) return -1;
+    unsigned long long n = 0;
+    if (cudaMemcpy(&n, b->nbad, sizeof(n), cudaMemcpyDeviceToHost) != cudaSuccess) return -1;
+    return (int64_t)n;
+}
+
+int lqt_batch_get_detect(lqt_batch *b, float *t_act, float *apd90, float *dvdt_max, uint8_t *ead, int32_t *nbeats)
+{
+    if (!b) return fail(LQT_ERR_INVALID, "lqt_batch_get_detect: NULL handle");
+    if (b->p.max_beats == 0) return fail(LQT_ERR_STATE, "lqt_batch_get_detect: created with max_beats = 0");
+    const int64_t n = b->ncells, nb = b->p.max_beats;
+    std::vector<float> buf((size_t)(n * nb));
+    auto fetch_f = [&](float *dst, const float *src) -> int {
+        if (!dst) return LQT_OK;
+        CK(cudaMemcpy(buf.data(), src, n * nb * 4, cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < n; ++i)
+            for (int64_t k = 0; k < nb; ++k) {
+                float x = buf[i * nb + k];
+                dst[b->perm[i] * nb + k] = (x == x) ? x : -1.f;
+            }
+        return LQT_OK;
+    };
+    int rc = fetch_f(t_act, b->det_t_act);
+    if (!rc) rc = fetch_f(apd90, b->det_apd90);
+    if (!rc) rc = fetch_f(dvdt_max, b->det_dvdt);
+    if (rc) return rc;
+    if (ead) {
+        std::vector<uint8_t> e(n);
+        CK(cudaMemcpy(e.data(), b->det_ead, n, cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < n; ++i) ead[b->perm[i]] = e[i];
+    }
+    if (nbeats) {
+        std::vector<int32_t> e(n);
+        CK(cudaMemcpy(e.data(), b->det_beats, n * 4, cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < n; ++i) nbeats[b->perm[i]] = e[i];
+    }
+    return LQT_OK;
+}
+
+int lqt_batch_get_record(lqt_batch *b, int32_t i, float *v, double *t, double *ecg, int64_t cap, int64_t *nrec)
+{
+    if (!b || i < 0 || i >= b->ninst) return fail(LQT_ERR_INVALID, "lqt_batch_get_record: bad handle or instance");
+    const int slot = b->rec_slot[i];
+    if (slot < 0) return fail(LQT_ERR_STATE, "lqt_batch_get_record: instance was not recorded");
+    const int64_t ns = b->inst_nsteps[i];
+    const int64_t nr = std::min<int64_t>((ns + b->p.rec_every - 1) / b->p.rec_every, b->rec_cap);
+    if (nrec) *nrec = nr;
+    const int64_t m = std::min(nr, cap);
+    const int n = b->inst[i].ncells;
+    if (v && m > 0) {
+        std::vector<float> buf((size_t)(m * b->rec_width));
+        CK(cudaMemcpy(buf.data(), b->rec_v + (int64_t)slot * b->rec_cap * b->rec_width, m * b->rec_width * 4,
+                      cudaMemcpyDeviceToHost));
+        for (int64_t r = 0; r < m; ++r) std::memcpy(v + r * n, &buf[r * b->rec_width], n * 4);
+    }
+    if (t && m > 0) CK(cudaMemcpy(t, b->rec_t + (int64_t)slot * b->rec_cap, m * 8, cudaMemcpyDeviceToHost));
+    if (ecg && m > 0) CK(cudaMemcpy(ecg, b->ecg + (int64_t)slot * b->rec_cap, m * 8, cudaMemcpyDeviceToHost));
+    return LQT_OK;
+}
+
+int lqt_batch_get_state(lqt_batch *b, double *state_host)
+{
+    if (!b || !state_host) return fail(LQT_ERR_INVALID, "lqt_batch_get_state: NULL");
+    cudaStream_t st = b->stream;
+    const int64_t ld = b->ld;
+    CK(b->p.precision == LQT_FP64
+           ? launch_unpack<double>(SoA<double>{(double *)b->v, b->conc, (double *)b->gate, ld}, b->aos, b->ncells, st)
+           : launch_unpack<float>(SoA<float>{(float *)b->v, b->conc, (float *)b->gate, ld}, b->aos, b->ncells, st));
+    std::vector<double> buf((size_t)b->ncells * 40);
+    CK(cudaMemcpyAsync(buf.data(), b->aos, b->ncells * 320, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    for (int64_t i = 0; i < b->ncells; ++i) std::memcpy(state_host + b->perm[i] * 40, &buf[i * 40], 320);
+    return LQT_OK;
+}
+
+int lqt_batch_set_state(lqt_batch *b, const double *state_host)
+{
+    if (!b || !state_host) return fail(LQT_ERR_INVALID, "lqt_batch_set_state: NULL");
+    cudaStream_t st = b->stream;
+    const int64_t ld = b->ld;
+    std::vector<double> buf((size_t)b->ncells * 40);
+    for (int64_t i = 0; i < b->ncells; ++i) std::memcpy(&buf[i * 40], state_host + b->perm[i] * 40, 320);
+    CK(cudaMemcpyAsync(b->aos, buf.data(), b->ncells * 320, cudaMemcpyHostToDevice, st));
+    CK(b->p.precision == LQT_FP64
+           ? launch_pack<double>(b->aos, SoA<double>{(double *)b->v, b->conc, (double *)b->gate, ld}, b->ncells, st)
+           : launch_pack<float>(b->aos, SoA<float>{(float *)b->v, b->conc, (float *)b->gate, ld}, b->ncells, st));
+    CK(cudaStreamSynchronize(st));
+    return LQT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,769 @@
+// api_sim.cu -- lqt_sim_*: 1D/2D/3D tissue simulations on one GPU.
+//
+// The host loop of the reference (GPU3D.cu:1731-1842, new_11.cu:1755-1890)
+// launches five kernels with a device-wide synchronisation between them and
+// copies all of V back every step.  Here a step is two kernels (k_grid_step,
+// k_ghost) on one stream; runs of steps are captured once into a CUDA graph
+// and replayed, the stimulus schedule and time live on the device, the
+// blow-up scan is a counter read on request, and the pseudo-ECG is reduced on
+// the device every `every` steps.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "api_common.h"
+#include "geometry.h"
+#include "grid_dev.h"
+
+using namespace lqt;
+
+namespace {
+constexpr int kGraphChunk = 50;   // steps per captured graph (even: V buffer parity is kept)
+constexpr uint32_t kCkptMagic = 0x4c515443;   // "LQTC"
+constexpr uint32_t kCkptVersion = 1;
+}  // namespace
+
+struct lqt_sim {
+    lqt_sim_params p{};
+    int32_t nx = 0, ny = 0, nz = 0, dim = 3;
+    double dx = 0.2;
+    int64_t ntissue = 0, ngrid = 0, nbnd = 0, ld = 0;
+    cudaStream_t stream = nullptr;
+    DevMem mem;
+    TissueMap tm;
+    // device
+    void *vg[2] = {nullptr, nullptr};
+    void *gate = nullptr, *d6 = nullptr, *b3 = nullptr, *coeff = nullptr, *dcoeff = nullptr;
+    double *conc = nullptr, *aos = nullptr;
+    int32_t *gidx = nullptr, *bnd_dst = nullptr, *bnd_src = nullptr;
+    uint8_t *ctl = nullptr;
+    float *onset = nullptr;
+    Clock *clk = nullptr;
+    Win *win = nullptr;
+    int64_t win_cap = 0;
+    float4 *det = nullptr;
+    float *apd90 = nullptr;
+    unsigned long long *nbad = nullptr;
+    // protocol
+    bool has_protocol = false, has_s2 = false;
+    bool own_stream = false;
+    lqt_protocol proto{};
+    std::vector<uint8_t> ctl_host;
+    int64_t win_horizon = 0;            // windows valid for steps < win_horizon
+    int32_t nwin = 0;
+    Win s2win{INT64_MAX, INT64_MAX};
+    std::vector<double> times;
+    // host mirror of the clock
+    int64_t step = 0;
+    double time = 0.0;
+    int cur = 0;
+    // ECG
+    int32_t nel = 0, ecg_every = 0;
+    float4 *el = nullptr;
+    double *ecg_partial = nullptr, *ecg_out = nullptr, *ecg_t = nullptr;
+    int64_t *ecg_count = nullptr, ecg_cap = 0;
+    // graph
+    cudaGraphExec_t graph = nullptr;
+    int graph_cur = -1;
+    bool graph_valid = false;
+
+    ~lqt_sim()
+    {
+        if (graph) cudaGraphExecDestroy(graph);
+        if (own_stream && stream) cudaStreamDestroy(stream);
+    }
+    bool fp64() const { return p.precision == LQT_FP64; }
+
+    template <typename R> GridDev<R> dev() const
+    {
+        GridDev<R> g{};
+        g.s = SoA<R>{nullptr, conc, (R *)gate, ld};
+        g.vg[0] = (R *)vg[0];
+        g.vg[1] = (R *)vg[1];
+        g.gidx = gidx;
+        g.ctl = ctl;
+        g.d6 = (const R *)d6;
+        g.b3 = (const R *)b3;
+        g.coeff = (const R *)coeff;
+        g.dcoeff = (const R *)dcoeff;
+        g.ntissue = ntissue;
+        g.nbnd = nbnd;
+        g.sx = (int64_t)ny * nz;
+        g.sy = dim == 2 ? 1 : nz;
+        g.pad = 0;
+        g.dx = dx;
+        g.inv_dx = 1.0 / dx;
+        g.inv_2dx = 1.0 / (2.0 * dx);
+        g.inv_dx2 = 1.0 / (dx * dx);
+        g.inv_4dx2 = 1.0 / (4.0 * dx * dx);
+        g.dt = p.dt;
+        g.model = make_modelk(p.model);
+        g.clk = clk;
+        g.win = win;
+        g.nwin = nwin;
+        g.s1_beats = proto.s1_beats;
+        g.s2_win = s2win;
+        g.bcl = has_protocol ? proto.bcl : 1.0;
+        g.s1_start = proto.s1_start;
+        g.s1_dur = proto.s1_duration;
+        g.s1_strength = proto.s1_strength;
+        g.s2_strength = proto.s2_strength;
+        g.onset = onset;
+        g.bnd_dst = bnd_dst;
+        g.bnd_src = bnd_src;
+        g.det = det;
+        g.apd90 = apd90;
+        g.act_thr = (float)p.act_threshold;
+        g.vmin_ok = p.vmin_ok;
+        g.vmax_ok = p.vmax_ok;
+        g.nbad = nbad;
+        return g;
+    }
+    double diso = 0.154;
+};
+
+namespace {
+
+template <typename R> GridDev<R> devf(const lqt_sim *s)
+{
+    GridDev<R> g = s->dev<R>();
+    g.diso = s->diso;
+    return g;
+}
+
+// Recompute S1 windows for steps [0, horizon) and the S2 window; upload.
+int refresh_windows(lqt_sim *s, int64_t horizon)
+{
+    if (!s->has_protocol) {
+        s->nwin = 0;
+        s->win_horizon = INT64_MAX;
+        return LQT_OK;
+    }
+    const lqt_protocol &q = s->proto;
+    const double t_end = horizon * s->p.dt + 10 * s->p.dt;
+    time_axis(s->p.dt, t_end, s->times);
+    const int64_t ns = std::min<int64_t>((int64_t)s->times.size(), horizon + 8);
+    std::vector<Win> w;
+    if (!s->onset) stim_windows(s->times, ns, s->p.dt, q.bcl, q.s1_start, q.s1_duration, q.s1_beats, w);
+    if ((int64_t)w.size() > s->win_cap) {
+        int64_t cap = std::max<int64_t>(64, (int64_t)w.size() * 2);
+        Win *nw = nullptr;
+        if (s->mem.alloc((void **)&nw, cap * sizeof(Win))) return LQT_ERR_NOMEM;
+        s->win = nw;
+        s->win_cap = cap;
+        s->graph_valid = false;
+    }
+    if (!w.empty()) CK(cudaMemcpyAsync(s->win, w.data(), w.size() * sizeof(Win), cudaMemcpyHostToDevice, s->stream));
+    if ((int32_t)w.size() != s->nwin) s->graph_valid = false;
+    s->nwin = (int32_t)w.size();
+    // S2: steps whose time is in [s2_time, s2_time + s2_duration)
+    Win s2{INT64_MAX, INT64_MAX};
+    if (s->has_s2 && q.s2_time >= 0 && q.s2_duration > 0) {
+        for (int64_t k = 0; k < ns; ++k) {
+            const double t = s->times[k];
+            const bool in = t >= q.s2_time && t < q.s2_time + q.s2_duration;
+            if (in && s2.on == INT64_MAX) s2.on = k;
+            if (!in && s2.on != INT64_MAX) {
+                s2.off = k;
+                break;
+            }
+        }
+        if (s2.on != INT64_MAX && s2.off == INT64_MAX) s2.off = ns;
+    }
+    if (s2.on != s->s2win.on || s2.off != s->s2win.off) s->graph_valid = false;
+    s->s2win = s2;
+    s->win_horizon = ns - 8;
+    // the device clock for the current step
+    Clock c{};
+    c.step = s->step;
+    c.time = s->time;
+    int32_t wi = 0;
+    while (wi < s->nwin && s->step >= w[wi].off) ++wi;
+    c.widx = wi;
+    c.s1_on = wi < s->nwin && s->step >= w[wi].on;
+    c.opened = wi < s->nwin && s->step == w[wi].on;
+    c.s2_on = s->step >= s2.on && s->step < s2.off;
+    c.tb = s->time - std::floor(s->time / q.bcl) * q.bcl;
+    c.s1_cycle_ok = q.s1_beats <= 0 || std::floor(s->time / q.bcl) < q.s1_beats;
+    CK(cudaMemcpyAsync(s->clk, &c, sizeof(c), cudaMemcpyHostToDevice, s->stream));
+    return LQT_OK;
+}
+
+int launch_step(lqt_sim *s)
+{
+    const StepK k = make_stepk(s->p.dt);
+    if (s->fp64()) {
+        const GridDev<double> g = devf<double>(s);
+        CK(launch_grid_step<double>(g, k, s->cur, s->dim, s->stream));
+        CK(launch_ghost<double>(g, s->cur ^ 1, s->stream));
+    } else {
+        const GridDev<float> g = devf<float>(s);
+        CK(launch_grid_step<float>(g, k, s->cur, s->dim, s->stream));
+        CK(launch_ghost<float>(g, s->cur ^ 1, s->stream));
+    }
+    s->cur ^= 1;
+    return LQT_OK;
+}
+
+int launch_ecg_now(lqt_sim *s)
+{
+    if (s->fp64())
+        CK(launch_ecg<double>(devf<double>(s), s->cur, s->el, s->nel, s->ecg_partial, s->ecg_out, s->ecg_t,
+                              s->ecg_count, s->ecg_cap, s->dim, s->stream));
+    else
+        CK(launch_ecg<float>(devf<float>(s), s->cur, s->el, s->nel, s->ecg_partial, s->ecg_out, s->ecg_t,
+                             s->ecg_count, s->ecg_cap, s->dim, s->stream));
+    return LQT_OK;
+}
+
+// One step plus, when due, an ECG sample of the new V.
+int step_once(lqt_sim *s)
+{
+    int rc = launch_step(s);
+    if (rc) return rc;
+    s->step += 1;
+    s->time += s->p.dt;
+    if (s->nel > 0 && s->ecg_every > 0 && s->step % s->ecg_every == 0) return launch_ecg_now(s);
+    return LQT_OK;
+}
+
+int build_graph(lqt_sim *s)
+{
+    if (s->graph) {
+        cudaGraphExecDestroy(s->graph);
+        s->graph = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    const int64_t step0 = s->step;
+    const double time0 = s->time;
+    const int cur0 = s->cur;
+    CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = LQT_OK;
+    // capture with step numbers aligned to the ECG cadence: the graph is
+    // replayed only from steps that are multiples of kGraphChunk
+    for (int i = 0; i < kGraphChunk && rc == LQT_OK; ++i) rc = step_once(s);
+    cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+    s->step = step0;
+    s->time = time0;
+    s->cur = cur0;
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return fail(LQT_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&s->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(LQT_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    s->graph_valid = true;
+    s->graph_cur = cur0;
+    return LQT_OK;
+}
+
+template <typename R> int upload_conv(lqt_sim *s, void *dst, const std::vector<float> &src)
+{
+    if (src.empty()) return LQT_OK;
+    if (sizeof(R) == 4) {
+        CK(cudaMemcpyAsync(dst, src.data(), src.size() * 4, cudaMemcpyHostToDevice, s->stream));
+    } else {
+        std::vector<double> d(src.begin(), src.end());
+        CK(cudaMemcpyAsync(dst, d.data(), d.size() * 8, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    return LQT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lqt_sim_create(const lqt_sim_params *params, const lqt_geometry *geom, lqt_sim **out)
+{
+    if (!out) return fail(LQT_ERR_INVALID, "lqt_sim_create: out is NULL");
+    *out = nullptr;
+    if (!params || !geom || !geom->cell_type) return fail(LQT_ERR_INVALID, "lqt_sim_create: NULL argument");
+    const lqt_sim_params &p = *params;
+    if (!(p.dt > 0) || !std::isfinite(p.dt)) return fail(LQT_ERR_INVALID, "lqt_sim_create: dt must be > 0");
+    if (p.precision != LQT_FP64 && p.precision != LQT_MIXED) return fail(LQT_ERR_INVALID, "lqt_sim_create: precision");
+    int rc = check_model(p.model);
+    if (rc) return rc;
+    const int32_t nx = geom->nx, ny = geom->ny, nz = geom->nz;
+    if (nx < 1 || ny < 1 || nz < 1 || (int64_t)nx * ny * nz > (int64_t)INT32_MAX)
+        return fail(LQT_ERR_INVALID, "lqt_sim_create: grid dimensions must be >= 1 and the grid below 2^31 voxels");
+    if (!(geom->dx > 0)) return fail(LQT_ERR_INVALID, "lqt_sim_create: dx must be > 0");
+    const int dim = (ny == 1 && nz == 1) ? 1 : (nz == 1 ? 2 : 3);
+    if (dim == 2 && ny < 3) return fail(LQT_ERR_INVALID, "lqt_sim_create: 2D grids need ny >= 3");
+    const int64_t total = (int64_t)nx * ny * nz;
+    for (int64_t i = 0; i < total; ++i)
+        if (geom->cell_type[i] > LQT_MCELL && geom->cell_type[i] != LQT_EMPTY)
+            return fail(LQT_ERR_INVALID, "lqt_sim_create: cell type out of range");
+    if (dim == 1) {
+        for (int64_t i = 0; i < total; ++i)
+            if (geom->cell_type[i] == LQT_EMPTY) return fail(LQT_ERR_INVALID, "lqt_sim_create: 1D strands must be all tissue");
+    } else {
+        // tissue must not touch the grid faces (the reference warns about it,
+        // GPU3D.cu:1287-1289); the stencil reads one voxel beyond tissue
+        for (int32_t x = 0; x < nx; ++x)
+            for (int32_t y = 0; y < ny; ++y)
+                for (int32_t z = 0; z < nz; ++z) {
+                    const bool face = x == 0 || x == nx - 1 || y == 0 || y == ny - 1 ||
+                                      (dim == 3 && (z == 0 || z == nz - 1));
+                    if (face && geom->cell_type[((int64_t)x * ny + y) * nz + z] != LQT_EMPTY)
+                        return fail(LQT_ERR_INVALID, "lqt_sim_create: tissue on the grid boundary; pad the grid by one empty voxel");
+                }
+    }
+    auto *s = new lqt_sim();
+    s->p = p;
+    s->nx = nx;
+    s->ny = ny;
+    s->nz = nz;
+    s->dim = dim;
+    s->dx = geom->dx;
+    s->stream = (cudaStream_t)p.stream;
+    if (!s->stream) {
+        // graph capture needs a stream other than the legacy default stream
+        if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete s;
+            return fail(LQT_ERR_CUDA, "lqt_sim_create: cannot create a stream");
+        }
+        s->own_stream = true;
+    }
+    if (!(s->p.vmin_ok < s->p.vmax_ok)) {
+        s->p.vmin_ok = -1e30;       // NaN-only check when no range is given
+        s->p.vmax_ok = 1e30;
+    }
+    s->diso = geom->d_fibre;
+    s->ngrid = total;
+    if (dim == 1) {
+        s->tm.cells.resize(nx);
+        s->tm.tissue_of.resize(nx);
+        for (int32_t i = 0; i < nx; ++i) {
+            s->tm.cells[i] = i;
+            s->tm.tissue_of[i] = i;
+        }
+    } else {
+        build_tissue_map(nx, ny, nz, geom->cell_type, s->tm);
+    }
+    s->ntissue = (int64_t)s->tm.cells.size();
+    s->nbnd = (int64_t)s->tm.bnd_dst.size();
+    if (s->ntissue == 0) {
+        delete s;
+        return fail(LQT_ERR_INVALID, "lqt_sim_create: no tissue voxels");
+    }
+    s->ld = pad128(s->ntissue);
+    const size_t rsz = s->fp64() ? 8 : 4;
+    const int64_t n = s->ntissue;
+    rc = 0;
+    rc |= s->mem.alloc(&s->vg[0], s->ngrid * rsz);
+    rc |= s->mem.alloc(&s->vg[1], s->ngrid * rsz);
+    rc |= s->mem.alloc(&s->gate, s->ld * rsz * kNGate);
+    rc |= s->mem.alloc((void **)&s->conc, s->ld * 8 * kNConc);
+    rc |= s->mem.alloc((void **)&s->ctl, n);
+    rc |= s->mem.alloc((void **)&s->clk, sizeof(Clock));
+    rc |= s->mem.alloc((void **)&s->nbad, sizeof(unsigned long long));
+    if (dim > 1) {
+        rc |= s->mem.alloc((void **)&s->gidx, n * 4);
+        rc |= s->mem.alloc((void **)&s->bnd_dst, std::max<int64_t>(1, s->nbnd) * 4);
+        rc |= s->mem.alloc((void **)&s->bnd_src, std::max<int64_t>(1, s->nbnd) * 4);
+    }
+    if (dim > 1 && geom->fibre) {
+        rc |= s->mem.alloc(&s->d6, n * 6 * rsz);
+        rc |= s->mem.alloc(&s->b3, n * 3 * rsz);
+    }
+    if (dim == 1) {
+        rc |= s->mem.alloc(&s->coeff, n * rsz);
+        rc |= s->mem.alloc(&s->dcoeff, n * rsz);
+    }
+    if (p.detect) {
+        rc |= s->mem.alloc((void **)&s->det, n * sizeof(float4));
+        rc |= s->mem.alloc((void **)&s->apd90, n * 4);
+    }
+    if (rc) {
+        std::string m = g_err;
+        delete s;
+        return fail(LQT_ERR_NOMEM, "lqt_sim_create: " + m);
+    }
+    cudaStream_t st = s->stream;
+    // per-voxel control bytes and maps
+    s->ctl_host.resize(n);
+    for (int64_t k = 0; k < n; ++k) s->ctl_host[k] = geom->cell_type[s->tm.cells[k]] & kCtlType;
+    std::vector<int32_t> gi32(dim > 1 ? n : 0), bd(s->nbnd), bs(s->nbnd);
+    for (int64_t k = 0; k < (int64_t)gi32.size(); ++k) gi32[k] = (int32_t)s->tm.cells[k];
+    for (int64_t j = 0; j < s->nbnd; ++j) {
+        bd[j] = (int32_t)s->tm.bnd_dst[j];
+        bs[j] = (int32_t)s->tm.bnd_src[j];
+    }
+    cudaError_t e = cudaMemcpyAsync(s->ctl, s->ctl_host.data(), n, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && dim > 1) e = cudaMemcpyAsync(s->gidx, gi32.data(), n * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && s->nbnd) e = cudaMemcpyAsync(s->bnd_dst, bd.data(), s->nbnd * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && s->nbnd) e = cudaMemcpyAsync(s->bnd_src, bs.data(), s->nbnd * 4, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        delete s;
+        return fail(LQT_ERR_CUDA, std::string("lqt_sim_create: ") + cudaGetErrorString(e));
+    }
+    if (dim > 1 && geom->fibre) {
+        std::vector<float> d6, b3;
+        build_tensor(nx, ny, nz, geom->dx, s->tm, geom->fibre, geom->d_fibre, geom->d_trans, d6, b3);
+        rc = s->fp64() ? (upload_conv<double>(s, s->d6, d6) | upload_conv<double>(s, s->b3, b3))
+                       : (upload_conv<float>(s, s->d6, d6) | upload_conv<float>(s, s->b3, b3));
+    }
+    if (!rc && dim == 1) {
+        // OneD.cc:108-131
+        std::vector<float> co(n), dco(n);
+        std::vector<double> cd(n);
+        for (int64_t i = 0; i < n; ++i) cd[i] = geom->coeff_1d ? geom->coeff_1d[i] : geom->d_fibre;
+        std::vector<double> dd(n);
+        for (int64_t i = 0; i < n; ++i) {
+            if (n == 1) dd[i] = 0;
+            else if (i == 0) dd[i] = (cd[i + 1] - cd[i]) / geom->dx;
+            else if (i == n - 1) dd[i] = (cd[i] - cd[i - 1]) / geom->dx;
+            else dd[i] = (cd[i + 1] - cd[i - 1]) / (2.0 * geom->dx);
+        }
+        if (s->fp64()) {
+            cudaMemcpyAsync(s->coeff, cd.data(), n * 8, cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(s->dcoeff, dd.data(), n * 8, cudaMemcpyHostToDevice, st);
+        } else {
+            for (int64_t i = 0; i < n; ++i) {
+                co[i] = (float)cd[i];
+                dco[i] = (float)dd[i];
+            }
+            cudaMemcpyAsync(s->coeff, co.data(), n * 4, cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(s->dcoeff, dco.data(), n * 4, cudaMemcpyHostToDevice, st);
+        }
+        if (cudaStreamSynchronize(st) != cudaSuccess) rc = LQT_ERR_CUDA;
+    }
+    if (rc) {
+        std::string m = g_err;
+        delete s;
+        return fail(rc, "lqt_sim_create: " + m);
+    }
+    // initial state everywhere, V0 in both grids (ghosts included)
+    std::vector<double> init((size_t)n * 40);
+    for (int64_t k = 0; k < n; ++k) initial_state(p.v0, &init[k * 40]);
+    rc = lqt_sim_set_state(s, init.data());
+    if (!rc) {
+        Clock c{};
+        c.s1_cycle_ok = 1;
+        cudaError_t e2 = cudaMemcpyAsync(s->clk, &c, sizeof(c), cudaMemcpyHostToDevice, st);
+        std::vector<float4> d0(s->det ? n : 0, make_float4(0.f, 0.f, -1.f, 0.f));
+        if (e2 == cudaSuccess && s->det) e2 = cudaMemcpyAsync(s->det, d0.data(), n * sizeof(float4), cudaMemcpyHostToDevice, st);
+        if (e2 == cudaSuccess && s->apd90) e2 = cudaMemsetAsync(s->apd90, 0xff, n * 4, st);
+        if (e2 == cudaSuccess) e2 = cudaMemsetAsync(s->nbad, 0, sizeof(unsigned long long), st);
+        if (e2 == cudaSuccess) e2 = cudaStreamSynchronize(st);
+        if (e2 != cudaSuccess) rc = fail(LQT_ERR_CUDA, cudaGetErrorString(e2));
+    }
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return LQT_OK;
+}
+
+void lqt_sim_destroy(lqt_sim *s) { delete s; }
+
+int64_t lqt_sim_num_tissue(const lqt_sim *s) { return s ? s->ntissue : -1; }
+
+int lqt_sim_tissue_index(const lqt_sim *s, int64_t *grid_index_host)
+{
+    if (!s || !grid_index_host) return fail(LQT_ERR_INVALID, "lqt_sim_tissue_index: NULL");
+    std::memcpy(grid_index_host, s->tm.cells.data(), s->ntissue * 8);
+    return LQT_OK;
+}
+
+double lqt_sim_time(const lqt_sim *s) { return s ? s->time : -1.0; }
+
+int lqt_sim_set_protocol(lqt_sim *s, const lqt_protocol *q)
+{
+    if (!s || !q) return fail(LQT_ERR_INVALID, "lqt_sim_set_protocol: NULL");
+    if (!(q->bcl > 0) || q->s1_duration < 0 || q->s1_beats < 0 || !q->s1_mask)
+        return fail(LQT_ERR_INVALID, "lqt_sim_set_protocol: bcl > 0, s1_duration >= 0, s1_beats >= 0, s1_mask required");
+    const int64_t n = s->ntissue;
+    std::vector<uint8_t> c(s->ctl_host);
+    std::vector<float> on;
+    for (int64_t k = 0; k < n; ++k) {
+        const int64_t g = s->tm.cells[k];
+        c[k] = (uint8_t)((c[k] & kCtlType) | (q->s1_mask[g] ? kCtlS1 : 0) | (q->s2_mask && q->s2_mask[g] ? kCtlS2 : 0));
+    }
+    if (q->s1_onset) {
+        on.resize(n);
+        for (int64_t k = 0; k < n; ++k) on[k] = q->s1_onset[s->tm.cells[k]];
+        if (!s->onset && s->mem.alloc((void **)&s->onset, n * 4)) return LQT_ERR_NOMEM;
+        CK(cudaMemcpyAsync(s->onset, on.data(), n * 4, cudaMemcpyHostToDevice, s->stream));
+    } else {
+        s->onset = nullptr;
+    }
+    CK(cudaMemcpyAsync(s->ctl, c.data(), n, cudaMemcpyHostToDevice, s->stream));
+    s->proto = *q;
+    s->proto.s1_mask = nullptr;     // masks are folded into the control bytes
+    s->proto.s2_mask = nullptr;
+    s->proto.s1_onset = nullptr;
+    s->has_s2 = q->s2_mask != nullptr;
+    s->has_protocol = true;
+    s->graph_valid = false;
+    int rc = refresh_windows(s, s->step + 200000);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(s->stream));
+    return LQT_OK;
+}
+
+int lqt_sim_step(lqt_sim *s, int64_t nsteps)
+{
+    if (!s || nsteps < 0) return fail(LQT_ERR_INVALID, "lqt_sim_step: NULL handle or nsteps < 0");
+    if (s->has_protocol && s->step + nsteps + kGraphChunk > s->win_horizon) {
+        int rc = refresh_windows(s, s->step + nsteps + 200000);
+        if (rc) return rc;
+    }
+    int64_t left = nsteps;
+    while (left > 0) {
+        // graph replay for whole chunks starting on a chunk boundary
+        if (left >= kGraphChunk && s->step % kGraphChunk == 0 &&
+            (s->ecg_every <= 0 || kGraphChunk % s->ecg_every == 0)) {
+            if (!s->graph_valid || s->graph_cur != s->cur) {
+                int rc = build_graph(s);
+                if (rc) return rc;
+            }
+            CK(cudaGraphLaunch(s->graph, s->stream));
+            s->step += kGraphChunk;
+            for (int i = 0; i < kGraphChunk; ++i) s->time += s->p.dt;
+            left -= kGraphChunk;
+            continue;
+        }
+        int rc = step_once(s);
+        if (rc) return rc;
+        --left;
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    return LQT_OK;
+}
+
+int lqt_sim_get_v(lqt_sim *s, void *v_host, int as_double)
+{
+    if (!s || !v_host) return fail(LQT_ERR_INVALID, "lqt_sim_get_v: NULL");
+    const int64_t n = s->ntissue;
+    const size_t esz = as_double ? 8 : 4;
+    void *tmp = s->aos;
+    if (!tmp) {
+        if (s->mem.alloc((void **)&s->aos, n * 320)) return LQT_ERR_NOMEM;
+        tmp = s->aos;
+    }
+    const int32_t *gi = s->dim > 1 ? s->gidx : nullptr;
+    if (s->fp64()) {
+        if (as_double) CK((launch_gather_v<double, double>((double *)s->vg[s->cur], gi, (double *)tmp, n, s->stream)));
+        else CK((launch_gather_v<double, float>((double *)s->vg[s->cur], gi, (float *)tmp, n, s->stream)));
+    } else {
+        if (as_double) CK((launch_gather_v<float, double>((float *)s->vg[s->cur], gi, (double *)tmp, n, s->stream)));
+        else CK((launch_gather_v<float, float>((float *)s->vg[s->cur], gi, (float *)tmp, n, s->stream)));
+    }
+    CK(cudaMemcpyAsync(v_host, tmp, n * esz, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return LQT_OK;
+}
+
+int lqt_sim_get_state(lqt_sim *s, double *state_host)
+{
+    if (!s || !state_host) return fail(LQT_ERR_INVALID, "lqt_sim_get_state: NULL");
+    const int64_t n = s->ntissue;
+    if (!s->aos && s->mem.alloc((void **)&s->aos, n * 320)) return LQT_ERR_NOMEM;
+    // V: gather into a temporary SoA v slot (the last block of aos), then unpack
+    void *vtmp = nullptr;
+    if (s->mem.alloc(&vtmp, n * 8)) return LQT_ERR_NOMEM;
+    const int32_t *gi = s->dim > 1 ? s->gidx : nullptr;
+    cudaError_t e;
+    if (s->fp64()) {
+        e = launch_gather_v<double, double>((double *)s->vg[s->cur], gi, (double *)vtmp, n, s->stream);
+        if (e == cudaSuccess) e = launch_unpack<double>(SoA<double>{(double *)vtmp, s->conc, (double *)s->gate, s->ld}, s->aos, n, s->stream);
+    } else {
+        e = launch_gather_v<float, float>((float *)s->vg[s->cur], gi, (float *)vtmp, n, s->stream);
+        if (e == cudaSuccess) e = launch_unpack<float>(SoA<float>{(float *)vtmp, s->conc, (float *)s->gate, s->ld}, s->aos, n, s->stream);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(state_host, s->aos, n * 320, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(vtmp);
+    s->mem.ptrs.erase(std::remove(s->mem.ptrs.begin(), s->mem.ptrs.end(), vtmp), s->mem.ptrs.end());
+    if (e != cudaSuccess) return fail(LQT_ERR_CUDA, std::string("lqt_sim_get_state: ") + cudaGetErrorString(e));
+    return LQT_OK;
+}
+
+int lqt_sim_set_state(lqt_sim *s, const double *state_host)
+{
+    if (!s || !state_host) return fail(LQT_ERR_INVALID, "lqt_sim_set_state: NULL");
+    const int64_t n = s->ntissue;
+    if (!s->aos && s->mem.alloc((void **)&s->aos, n * 320)) return LQT_ERR_NOMEM;
+    void *vtmp = nullptr;
+    if (s->mem.alloc(&vtmp, n * 8)) return LQT_ERR_NOMEM;
+    const int32_t *gi = s->dim > 1 ? s->gidx : nullptr;
+    const size_t rsz = s->fp64() ? 8 : 4;
+    cudaError_t e = cudaMemcpyAsync(s->aos, state_host, n * 320, cudaMemcpyHostToDevice, s->stream);
+    // empty voxels that are not mirrored are never read; zero both grids
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->vg[0], 0, s->ngrid * rsz, s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->vg[1], 0, s->ngrid * rsz, s->stream);
+    if (s->fp64()) {
+        if (e == cudaSuccess) e = launch_pack<double>(s->aos, SoA<double>{(double *)vtmp, s->conc, (double *)s->gate, s->ld}, n, s->stream);
+        if (e == cudaSuccess) e = launch_scatter_v<double>((double *)vtmp, gi, (double *)s->vg[s->cur], n, s->stream);
+        if (e == cudaSuccess) e = launch_ghost<double>(s->dev<double>(), s->cur, s->stream);
+    } else {
+        if (e == cudaSuccess) e = launch_pack<float>(s->aos, SoA<float>{(float *)vtmp, s->conc, (float *)s->gate, s->ld}, n, s->stream);
+        if (e == cudaSuccess) e = launch_scatter_v<float>((float *)vtmp, gi, (float *)s->vg[s->cur], n, s->stream);
+        if (e == cudaSuccess) e = launch_ghost<float>(s->dev<float>(), s->cur, s->stream);
+    }
+    // launch_ghost also advanced the device clock: restore it
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    cudaFree(vtmp);
+    s->mem.ptrs.erase(std::remove(s->mem.ptrs.begin(), s->mem.ptrs.end(), vtmp), s->mem.ptrs.end());
+    if (e != cudaSuccess) return fail(LQT_ERR_CUDA, std::string("lqt_sim_set_state: ") + cudaGetErrorString(e));
+    if (s->has_protocol) return refresh_windows(s, std::max<int64_t>(s->win_horizon, s->step + 1000));
+    Clock c{};
+    c.step = s->step;
+    c.time = s->time;
+    c.s1_cycle_ok = 1;
+    CK(cudaMemcpy(s->clk, &c, sizeof(c), cudaMemcpyHostToDevice));
+    return LQT_OK;
+}
+
+int lqt_sim_set_electrodes(lqt_sim *s, int32_t n, const double *xyz, int32_t every)
+{
+    if (!s || n < 0 || n > kMaxElectrodes || (n > 0 && (!xyz || every <= 0)))
+        return fail(LQT_ERR_INVALID, "lqt_sim_set_electrodes: 0..8 electrodes, every > 0");
+    if (n > 0 && kGraphChunk % every != 0 && every % kGraphChunk != 0)
+        return fail(LQT_ERR_INVALID, "lqt_sim_set_electrodes: `every` must divide 50 or be a multiple of 50");
+    s->nel = n;
+    s->ecg_every = every;
+    s->graph_valid = false;
+    if (n == 0) return LQT_OK;
+    std::vector<float4> el(n);
+    for (int i = 0; i < n; ++i) el[i] = make_float4((float)xyz[3 * i], (float)xyz[3 * i + 1], (float)xyz[3 * i + 2], 0.f);
+    if (!s->el) {
+        int rc = s->mem.alloc((void **)&s->el, kMaxElectrodes * sizeof(float4)) |
+                 s->mem.alloc((void **)&s->ecg_partial, ecg_blocks(s->ntissue) * kMaxElectrodes * 8) |
+                 s->mem.alloc((void **)&s->ecg_count, 8);
+        if (rc) return LQT_ERR_NOMEM;
+    }
+    s->ecg_cap = 1 << 16;
+    if (!s->ecg_out) {
+        int rc = s->mem.alloc((void **)&s->ecg_out, s->ecg_cap * kMaxElectrodes * 8) |
+                 s->mem.alloc((void **)&s->ecg_t, s->ecg_cap * 8);
+        if (rc) return LQT_ERR_NOMEM;
+    }
+    CK(cudaMemcpyAsync(s->el, el.data(), n * sizeof(float4), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemsetAsync(s->ecg_count, 0, 8, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return LQT_OK;
+}
+
+int lqt_sim_get_ecg(lqt_sim *s, int64_t max_samples, double *phi, double *t, int64_t *nsamples)
+{
+    if (!s) return fail(LQT_ERR_INVALID, "lqt_sim_get_ecg: NULL");
+    if (s->nel == 0) return fail(LQT_ERR_STATE, "lqt_sim_get_ecg: no electrodes set");
+    int64_t cnt = 0;
+    CK(cudaMemcpy(&cnt, s->ecg_count, 8, cudaMemcpyDeviceToHost));
+    if (nsamples) *nsamples = cnt;
+    const int64_t m = std::min(cnt, max_samples);
+    if (m > 0 && phi) {
+        std::vector<double> buf(m * s->nel);
+        CK(cudaMemcpy(buf.data(), s->ecg_out, m * s->nel * 8, cudaMemcpyDeviceToHost));
+        std::memcpy(phi, buf.data(), m * s->nel * 8);
+    }
+    if (m > 0 && t) CK(cudaMemcpy(t, s->ecg_t, m * 8, cudaMemcpyDeviceToHost));
+    return LQT_OK;
+}
+
+int lqt_sim_get_detect(lqt_sim *s, float *t_act, float *apd90, uint8_t *ead)
+{
+    if (!s) return fail(LQT_ERR_INVALID, "lqt_sim_get_detect: NULL");
+    if (!s->det) return fail(LQT_ERR_STATE, "lqt_sim_get_detect: created with detect = 0");
+    const int64_t n = s->ntissue;
+    std::vector<float4> d(n);
+    CK(cudaMemcpy(d.data(), s->det, n * sizeof(float4), cudaMemcpyDeviceToHost));
+    for (int64_t k = 0; k < n; ++k) {
+        uint32_t bits;
+        std::memcpy(&bits, &d[k].w, 4);
+        if (t_act) t_act[k] = d[k].z;
+        if (ead) ead[k] = (bits >> 3) & 1u;
+    }
+    if (apd90) {
+        CK(cudaMemcpy(apd90, s->apd90, n * 4, cudaMemcpyDeviceToHost));
+        for (int64_t k = 0; k < n; ++k)
+            if (!(apd90[k] == apd90[k])) apd90[k] = -1.f;
+    }
+    return LQT_OK;
+}
+
+int lqt_sim_boundary(const lqt_sim *s, int64_t *dst, int64_t *src, int64_t *n)
+{
+    if (!s || !n) return fail(LQT_ERR_INVALID, "lqt_sim_boundary: NULL");
+    *n = s->nbnd;
+    if (dst) std::memcpy(dst, s->tm.bnd_dst.data(), s->nbnd * 8);
+    if (src) std::memcpy(src, s->tm.bnd_src.data(), s->nbnd * 8);
+    return LQT_OK;
+}
+
+int lqt_sim_check(lqt_sim *s, int64_t *n_bad)
+{
+    if (!s || !n_bad) return fail(LQT_ERR_INVALID, "lqt_sim_check: NULL");
+    unsigned long long v = 0;
+    CK(cudaMemcpy(&v, s->nbad, sizeof(v), cudaMemcpyDeviceToHost));
+    CK(cudaMemset(s->nbad, 0, sizeof(v)));
+    *n_bad = (int64_t)v;
+    return v ? LQT_ERR_NUMERIC : LQT_OK;
+}
+
+int lqt_sim_checkpoint(lqt_sim *s, const char *path)
+{
+    if (!s || !path) return fail(LQT_ERR_INVALID, "lqt_sim_checkpoint: NULL");
+    std::vector<double> st((size_t)s->ntissue * 40);
+    int rc = lqt_sim_get_state(s, st.data());
+    if (rc) return rc;
+    FILE *f = std::fopen(path, "wb");
+    if (!f) return fail(LQT_ERR_IO, std::string("lqt_sim_checkpoint: cannot open ") + path);
+    const uint32_t hdr[4] = {kCkptMagic, kCkptVersion, (uint32_t)s->p.precision, (uint32_t)s->dim};
+    const int64_t dims[4] = {s->nx, s->ny, s->nz, s->ntissue};
+    bool ok = std::fwrite(hdr, sizeof(hdr), 1, f) == 1 && std::fwrite(dims, sizeof(dims), 1, f) == 1 &&
+              std::fwrite(&s->step, 8, 1, f) == 1 && std::fwrite(&s->time, 8, 1, f) == 1;
+    // per-state arrays (state-major) so a field can be read without the rest
+    std::vector<double> col(s->ntissue);
+    for (int j = 0; j < 40 && ok; ++j) {
+        for (int64_t k = 0; k < s->ntissue; ++k) col[k] = st[k * 40 + j];
+        ok = std::fwrite(col.data(), 8, s->ntissue, f) == (size_t)s->ntissue;
+    }
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? LQT_OK : fail(LQT_ERR_IO, "lqt_sim_checkpoint: write failed");
+}
+
+int lqt_sim_restore(lqt_sim *s, const char *path)
+{
+    if (!s || !path) return fail(LQT_ERR_INVALID, "lqt_sim_restore: NULL");
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return fail(LQT_ERR_IO, std::string("lqt_sim_restore: cannot open ") + path);
+    uint32_t hdr[4];
+    int64_t dims[4], step = 0;
+    double time = 0;
+    bool ok = std::fread(hdr, sizeof(hdr), 1, f) == 1 && std::fread(dims, sizeof(dims), 1, f) == 1 &&
+              std::fread(&step, 8, 1, f) == 1 && std::fread(&time, 8, 1, f) == 1;
+    if (!ok || hdr[0] != kCkptMagic || hdr[1] != kCkptVersion) {
+        std::fclose(f);
+        return fail(LQT_ERR_IO, "lqt_sim_restore: not an lqt checkpoint (bad magic or version)");
+    }
+    if (dims[0] != s->nx || dims[1] != s->ny || dims[2] != s->nz || dims[3] != s->ntissue) {
+        std::fclose(f);
+        return fail(LQT_ERR_INVALID, "lqt_sim_restore: checkpoint geometry differs from this simulation");
+    }
+    std::vector<double> st((size_t)s->ntissue * 40), col(s->ntissue);
+    for (int j = 0; j < 40 && ok; ++j) {
+        ok = std::fread(col.data(), 8, s->ntissue, f) == (size_t)s->ntissue;
+        for (int64_t k = 0; k < s->ntissue && ok; ++k) st[k * 40 + j] = col[k];
+    }
+    std::fclose(f);
+    if (!ok) return fail(LQT_ERR_IO, "lqt_sim_restore: truncated checkpoint");
+    s->step = step;
+    s->time = time;
+    s->graph_valid = false;
+    return lqt_sim_set_state(s, st.data());
+}
+
+}  // extern "C"

@@ -1,0 +1,63 @@
+// grid_dev.h -- device view of a tissue grid simulation (k_grid.cuh, api_sim.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lqt_internal.h"
+
+namespace lqt {
+
+constexpr uint8_t kCtlType = 7;    // bits 0-2: LQT_* cell type (0..4)
+constexpr uint8_t kCtlS1 = 8;      // receives S1
+constexpr uint8_t kCtlS2 = 16;     // receives S2
+constexpr int kMaxElectrodes = 8;
+
+// Per-step control, advanced on the device by k_ghost so that a run of steps
+// can be captured in one CUDA graph.
+struct Clock {
+    int64_t step;
+    double time;        // accumulated as `time += dt` (OneD.cc:317)
+    double tb;          // time - floor(time/bcl)*bcl (only kept with onsets)
+    int32_t widx;       // current S1 window
+    int32_t s1_on, s2_on, opened, s1_cycle_ok, pad;
+};
+
+template <typename R> struct GridDev {
+    SoA<R> s;                      // per tissue voxel
+    R *vg[2];                      // dense V grids (1D: tissue order)
+    const int32_t *gidx;           // tissue -> dense index
+    const uint8_t *ctl;            // type + stimulus bits
+    const R *d6, *b3;              // anisotropic tensor and its divergence, or null
+    const R *coeff, *dcoeff;       // 1D: D and dD/dx per cell
+    double diso;                   // isotropic D
+    int64_t ntissue, nbnd;
+    int64_t sx, sy;                // dense strides of x and y (z stride 1)
+    int64_t pad;                   // grid origin offset (0)
+    double dx, inv_dx, inv_2dx, inv_dx2, inv_4dx2;
+    double dt;
+    ModelK model;
+    Clock *clk;
+    const Win *win;                // S1 windows
+    int32_t nwin;
+    int32_t s1_beats;
+    Win s2_win;
+    double bcl, s1_start, s1_dur;
+    double s1_strength, s2_strength;
+    const float *onset;            // per tissue voxel onset delay, or null
+    const int32_t *bnd_dst, *bnd_src;
+    float4 *det;                   // {vrest, vpeak, t_act, bits}, or null
+    float *apd90;
+    float act_thr;
+    double vmin_ok, vmax_ok;
+    unsigned long long *nbad;
+};
+
+template <typename R>
+cudaError_t launch_grid_step(const GridDev<R> &gd, const StepK &k, int cur, int dim, cudaStream_t st);
+template <typename R> cudaError_t launch_ghost(const GridDev<R> &gd, int nxt, cudaStream_t st);
+template <typename R>
+cudaError_t launch_ecg(const GridDev<R> &gd, int cur, const float4 *el, int nel, double *partial, double *out,
+                       double *t_out, int64_t *counter, int64_t cap, int dim, cudaStream_t st);
+int64_t ecg_blocks(int64_t ntissue);
+
+}  // namespace lqt

@@ -1,0 +1,228 @@
+// k_grid.cuh -- fused diffusion + stimulus + TPORd step on 1D/2D/3D grids.
+//
+// Replaces the reference's per-step kernel chain calc_du -> init_Istim ->
+// set_Istim -> Itot -> new_u_v (GPU3D.cu:370-425,1222-1230; new_11.cu:352-455,
+// 1241-1255) with one kernel per step plus a small ghost-fill kernel.
+//
+// Layout: V lives in a dense grid (x-major, z fastest, as GPU3D.cu:29-33),
+// double-buffered; the other 39 states live in structure-of-arrays order over
+// the tissue voxels (common.cuh).  One thread per tissue voxel: it reads its V
+// stencil from the dense grid (neighbour rows are shared through L1/L2), its
+// state with streaming loads, and writes V into the other grid.  Empty voxels
+// next to tissue hold the V of their mirror source (GPU3D.cu:1487-1604),
+// refreshed after every step by k_ghost, so the stencil needs no branches.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "grid_dev.h"
+
+namespace lqt {
+
+// du = sum_i D_ii V_ii + 2 sum_{i<j} D_ij V_ij + sum_j b_j V_j
+// (new_11.cu:352-417 in 2D; 7-point D*lap(V) when isotropic, GPU3D.cu:370-385).
+template <typename R, int DIM>
+__device__ __forceinline__ R grid_du(const GridDev<R> &gd, const R *__restrict__ V, int64_t g, int64_t k, R vc)
+{
+    if constexpr (DIM == 1) {
+        // OneD.cc:371-391: mirrored ends, dD/dx term
+        const int64_t n = gd.ntissue;
+        R fo, so;
+        if (n == 1) return (R)0;
+        if (g == 0) {
+            const R vp = V[g + 1];
+            fo = (vp - vc) * (R)gd.inv_dx;
+            so = (vp + vc - (R)2 * vc) * (R)gd.inv_dx2;
+        } else if (g == n - 1) {
+            const R vm = V[g - 1];
+            fo = (vc - vm) * (R)gd.inv_dx;
+            so = (vc + vm - (R)2 * vc) * (R)gd.inv_dx2;
+        } else {
+            const R vp = V[g + 1], vm = V[g - 1];
+            fo = (vp - vm) * (R)gd.inv_2dx;
+            so = (vp + vm - (R)2 * vc) * (R)gd.inv_dx2;
+        }
+        return (R)gd.dcoeff[k] * fo + (R)gd.coeff[k] * so;
+    } else {
+        const int64_t sx = gd.sx, sy = gd.sy;
+        const R vxp = V[g + sx], vxm = V[g - sx], vyp = V[g + sy], vym = V[g - sy];
+        const R c2 = (R)gd.inv_dx2;
+        const R lxx = (vxp + vxm - (R)2 * vc) * c2;
+        const R lyy = (vyp + vym - (R)2 * vc) * c2;
+        R lzz = 0, vzp = 0, vzm = 0;
+        if constexpr (DIM == 3) {
+            vzp = V[g + 1];
+            vzm = V[g - 1];
+            lzz = (vzp + vzm - (R)2 * vc) * c2;
+        }
+        if (!gd.d6) return (R)gd.diso * (lxx + lyy + lzz);
+        const R *D = gd.d6 + 6 * k;
+        const R *B = gd.b3 + 3 * k;
+        const R c4 = (R)gd.inv_4dx2, c1 = (R)gd.inv_2dx;
+        const R lxy = (V[g + sx + sy] + V[g - sx - sy] - V[g - sx + sy] - V[g + sx - sy]) * c4;
+        R du = D[0] * lxx + D[1] * lyy + (R)2 * D[3] * lxy + B[0] * ((vxp - vxm) * c1) + B[1] * ((vyp - vym) * c1);
+        if constexpr (DIM == 3) {
+            const R lxz = (V[g + sx + 1] + V[g - sx - 1] - V[g - sx + 1] - V[g + sx - 1]) * c4;
+            const R lyz = (V[g + sy + 1] + V[g - sy - 1] - V[g - sy + 1] - V[g + sy - 1]) * c4;
+            du += D[2] * lzz + (R)2 * (D[4] * lxz + D[5] * lyz) + B[2] * ((vzp - vzm) * c1);
+        }
+        return du;
+    }
+}
+
+template <typename R, int DIM>
+__global__ void __launch_bounds__(256) k_grid_step(GridDev<R> gd, StepK kst, int cur)
+{
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= gd.ntissue) return;
+    const Clock ck = *gd.clk;
+    const R *__restrict__ V = gd.vg[cur];
+    R *__restrict__ Vn = gd.vg[cur ^ 1];
+    const int64_t g = DIM == 1 ? k : (int64_t)gd.gidx[k];
+    const R vc = V[g];
+    const R du = grid_du<R, DIM>(gd, V, g, k, vc);
+
+    const uint8_t ctl = gd.ctl[k];
+    R ist = 0;
+    if (gd.onset) {
+        // per-voxel onset within each cycle (GPU3D.cu:397-409)
+        const double on = gd.s1_start + (double)gd.onset[k];
+        if ((ctl & kCtlS1) && ck.s1_cycle_ok && ck.tb >= on && ck.tb < on + gd.s1_dur) ist = (R)gd.s1_strength;
+    } else if (ck.s1_on && (ctl & kCtlS1)) {
+        ist = (R)gd.s1_strength;
+    }
+    if (ck.s2_on && (ctl & kCtlS2)) ist = (R)gd.s2_strength;
+
+    CellState<R> c;
+    load_cell(c, gd.s, k);
+    c.v = vc;
+    StepOut o{0.0};
+    tpord_step<R>(c, ctl & kCtlType, gd.model, kst, ist, du, &o);
+    store_cell(c, gd.s, k);
+    Vn[g] = c.v;
+
+    if (gd.det) {
+        float4 d = gd.det[k];
+        DetState ds;
+        ds.vrest = d.x;
+        ds.vpeak = d.y;
+        uint32_t bits = __float_as_uint(d.w);
+        ds.phase = bits & 7u;
+        ds.ead = (bits >> 3) & 1u;
+        ds.dvdt_max = 0.f;
+        float t_act = d.z;
+        bool dirty = false;
+        if (ck.opened) {
+            det_open_cycle(ds, (float)vc);
+            dirty = true;
+        }
+        if (ds.phase != kDetIdle && ds.phase != kDetDone) {
+            DetEvent ev;
+            const uint8_t ph0 = ds.phase;
+            const float vp0 = ds.vpeak;
+            const uint8_t e0 = ds.ead;
+            if (det_step(ds, (float)vc, (float)c.v, (float)o.dvdt, (float)ck.time, gd.act_thr, t_act, ev)) {
+                if (ev.t_90 >= 0.f) gd.apd90[k] = ev.apd90;
+            }
+            dirty |= ds.phase != ph0 || ds.vpeak != vp0 || ds.ead != e0;
+        }
+        if (dirty) {
+            const uint32_t nb = (bits >> 4) + (ck.opened ? 1u : 0u);
+            gd.det[k] = make_float4(ds.vrest, ds.vpeak, t_act, __uint_as_float((nb << 4) | (ds.ead << 3) | ds.phase));
+        }
+    }
+    const R vn = c.v;
+    const bool bad = !(vn == vn) || vn < (R)gd.vmin_ok || vn > (R)gd.vmax_ok;
+    const unsigned m = __ballot_sync(__activemask(), bad);
+    if (m && (threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(gd.nbad, (unsigned long long)__popc(m));
+}
+
+// Mirror-boundary refresh of the new grid, then the clock advance for the
+// next step (block 0, thread 0).
+template <typename R>
+__global__ void __launch_bounds__(256) k_ghost(GridDev<R> gd, int nxt)
+{
+    R *V = gd.vg[nxt];
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < gd.nbnd; j += (int64_t)gridDim.x * blockDim.x)
+        V[gd.bnd_dst[j]] = V[gd.bnd_src[j]];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        Clock ck = *gd.clk;
+        ck.step += 1;
+        ck.time += gd.dt;
+        int32_t w = ck.widx;
+        while (w < gd.nwin && ck.step >= gd.win[w].off) ++w;
+        ck.widx = w;
+        ck.s1_on = w < gd.nwin && ck.step >= gd.win[w].on;
+        ck.opened = w < gd.nwin && ck.step == gd.win[w].on;
+        ck.s2_on = ck.step >= gd.s2_win.on && ck.step < gd.s2_win.off;
+        if (gd.onset) {
+            ck.tb = ck.time - floor(ck.time / gd.bcl) * gd.bcl;
+            ck.s1_cycle_ok = gd.s1_beats <= 0 || floor(ck.time / gd.bcl) < gd.s1_beats;
+        }
+        *gd.clk = ck;
+    }
+}
+
+// Pseudo-ECG partial sums: 3D form of PlotScript/plot1DECG_compare.py:89-105,
+// phi(r0) = sum_i sum_axis (V[i+e] - V[i-e])/2 (r_i - r0)_axis / |r_i - r0|^3.
+// One FP64 partial per block and electrode, reduced in a fixed order by
+// k_ecg_final so the result does not depend on scheduling.
+template <typename R, int DIM>
+__global__ void __launch_bounds__(256) k_ecg_partial(GridDev<R> gd, const R *__restrict__ V,
+                                                     const float4 *__restrict__ el, int nel,
+                                                     double *__restrict__ partial)
+{
+    __shared__ double red[8][8];
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    float acc[kMaxElectrodes];
+#pragma unroll
+    for (int e = 0; e < kMaxElectrodes; ++e) acc[e] = 0.f;
+    if (k < gd.ntissue) {
+        const int64_t g = DIM == 1 ? k : (int64_t)gd.gidx[k];
+        float p[3] = {0.f, 0.f, 0.f}, h[3] = {0.f, 0.f, 0.f};
+        if constexpr (DIM == 1) {
+            p[0] = (float)(k * gd.dx);
+            const int64_t n = gd.ntissue;
+            if (n > 1) h[0] = k == 0 ? (float)(V[1] - V[0]) : (k == n - 1 ? (float)(V[k] - V[k - 1]) : 0.5f * (float)(V[k + 1] - V[k - 1]));
+        } else {
+            const int64_t x = g / gd.sx, rem = g - x * gd.sx;
+            const int64_t y = rem / gd.sy, z = rem - y * gd.sy;
+            p[0] = (float)((x - gd.pad) * gd.dx);
+            p[1] = (float)((y - gd.pad) * gd.dx);
+            p[2] = (float)((DIM == 3 ? z - gd.pad : 0) * gd.dx);
+            h[0] = 0.5f * (float)(V[g + gd.sx] - V[g - gd.sx]);
+            h[1] = 0.5f * (float)(V[g + gd.sy] - V[g - gd.sy]);
+            if constexpr (DIM == 3) h[2] = 0.5f * (float)(V[g + 1] - V[g - 1]);
+        }
+#pragma unroll
+        for (int e = 0; e < kMaxElectrodes; ++e) {
+            if (e < nel) {
+                const float rx = p[0] - el[e].x, ry = p[1] - el[e].y, rz = p[2] - el[e].z;
+                const float r2 = rx * rx + ry * ry + rz * rz;
+                const float inv = rsqrtf(r2);
+                acc[e] = (h[0] * rx + h[1] * ry + h[2] * rz) * (inv * inv * inv);
+            }
+        }
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int e = 0; e < kMaxElectrodes; ++e) {
+        if (e >= nel) break;
+        double v = (double)acc[e];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[wid][e] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < nel) {
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w][threadIdx.x];
+        partial[(int64_t)blockIdx.x * nel + threadIdx.x] = s;
+    }
+}
+
+__global__ void k_ecg_final(const double *__restrict__ partial, int64_t nblocks, int nel, double *__restrict__ out,
+                            double *__restrict__ t_out, int64_t *__restrict__ counter, int64_t cap,
+                            const Clock *__restrict__ clk);
+
+}  // namespace lqt

@@ -1,0 +1,71 @@
+// k_grid_f32.cu -- instantiations of the grid kernels (k_grid.cuh) for R = float.
+#include "k_grid.cuh"
+
+namespace lqt {
+
+template <>
+cudaError_t launch_grid_step<float>(const GridDev<float> &gd, const StepK &k, int cur, int dim, cudaStream_t st)
+{
+    if (gd.ntissue <= 0) return cudaSuccess;
+    const unsigned nb = (unsigned)((gd.ntissue + 255) / 256);
+    if (dim == 1) k_grid_step<float, 1><<<nb, 256, 0, st>>>(gd, k, cur);
+    else if (dim == 2) k_grid_step<float, 2><<<nb, 256, 0, st>>>(gd, k, cur);
+    else k_grid_step<float, 3><<<nb, 256, 0, st>>>(gd, k, cur);
+    return cudaGetLastError();
+}
+
+template <> cudaError_t launch_ghost<float>(const GridDev<float> &gd, int nxt, cudaStream_t st)
+{
+    int64_t nb = (gd.nbnd + 255) / 256;
+    if (nb < 1) nb = 1;
+    if (nb > 152 * 16) nb = 152 * 16;
+    k_ghost<float><<<(unsigned)nb, 256, 0, st>>>(gd, nxt);
+    return cudaGetLastError();
+}
+
+template <>
+cudaError_t launch_ecg<float>(const GridDev<float> &gd, int cur, const float4 *el, int nel, double *partial, double *out,
+                           double *t_out, int64_t *counter, int64_t cap, int dim, cudaStream_t st)
+{
+    const int64_t nb = ecg_blocks(gd.ntissue);
+    if (dim == 1) k_ecg_partial<float, 1><<<(unsigned)nb, 256, 0, st>>>(gd, gd.vg[cur], el, nel, partial);
+    else if (dim == 2) k_ecg_partial<float, 2><<<(unsigned)nb, 256, 0, st>>>(gd, gd.vg[cur], el, nel, partial);
+    else k_ecg_partial<float, 3><<<(unsigned)nb, 256, 0, st>>>(gd, gd.vg[cur], el, nel, partial);
+    k_ecg_final<<<1, 256, 0, st>>>(partial, nb, nel, out, t_out, counter, cap, gd.clk);
+    return cudaGetLastError();
+}
+
+}  // namespace lqt
+
+namespace lqt {
+
+int64_t ecg_blocks(int64_t ntissue) { return ntissue <= 0 ? 1 : (ntissue + 255) / 256; }
+
+// Sum the per-block partials of each electrode in block order (deterministic).
+__global__ void k_ecg_final(const double *__restrict__ partial, int64_t nblocks, int nel, double *__restrict__ out,
+                            double *__restrict__ t_out, int64_t *__restrict__ counter, int64_t cap,
+                            const Clock *__restrict__ clk)
+{
+    __shared__ double red[256];
+    const int64_t slot = *counter;
+    if (slot >= cap) return;
+    out += slot * nel;
+    for (int e = 0; e < nel; ++e) {
+        double s = 0.0;
+        for (int64_t b = threadIdx.x; b < nblocks; b += blockDim.x) s += partial[b * nel + e];
+        red[threadIdx.x] = s;
+        __syncthreads();
+        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+            if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[e] = red[0];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        t_out[slot] = clk->time;
+        *counter = slot + 1;
+    }
+}
+
+}  // namespace lqt

@@ -1,0 +1,94 @@
+// k_util.cu -- state conversion between the reference's per-cell order
+// (40 doubles, TPORd::outputAllStates order, SingleCell/TPORd.cc:200-252) and
+// the device structure of arrays.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace lqt {
+
+template <typename R>
+__global__ void k_pack(const double *__restrict__ aos, SoA<R> s, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double *a = aos + i * 40;
+        s.v[i] = (R)a[0];
+        for (int j = 0; j < kNConc; ++j) s.conc[j * s.ld + i] = a[1 + j];
+        for (int j = 0; j < kNGate; ++j) s.gate[j * s.ld + i] = (R)a[9 + j];
+    }
+}
+
+template <typename R>
+__global__ void k_unpack(SoA<R> s, double *__restrict__ aos, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double *a = aos + i * 40;
+        a[0] = (double)s.v[i];
+        for (int j = 0; j < kNConc; ++j) a[1 + j] = s.conc[j * s.ld + i];
+        for (int j = 0; j < kNGate; ++j) a[9 + j] = (double)s.gate[j * s.ld + i];
+    }
+}
+
+static unsigned grid_for(int64_t n, int bs)
+{
+    int64_t nb = (n + bs - 1) / bs;
+    return (unsigned)(nb < 1 ? 1 : (nb > 152 * 32 ? 152 * 32 : nb));
+}
+
+template <typename R> cudaError_t launch_pack(const double *aos, const SoA<R> &s, int64_t n, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    k_pack<R><<<grid_for(n, 256), 256, 0, st>>>(aos, s, n);
+    return cudaGetLastError();
+}
+template <typename R> cudaError_t launch_unpack(const SoA<R> &s, double *aos, int64_t n, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    k_unpack<R><<<grid_for(n, 256), 256, 0, st>>>(s, aos, n);
+    return cudaGetLastError();
+}
+template cudaError_t launch_pack<double>(const double *, const SoA<double> &, int64_t, cudaStream_t);
+template cudaError_t launch_pack<float>(const double *, const SoA<float> &, int64_t, cudaStream_t);
+template cudaError_t launch_unpack<double>(const SoA<double> &, double *, int64_t, cudaStream_t);
+template cudaError_t launch_unpack<float>(const SoA<float> &, double *, int64_t, cudaStream_t);
+
+}  // namespace lqt
+
+namespace lqt {
+
+// V of tissue voxels <-> dense grid.
+template <typename R, typename T>
+__global__ void k_gather_v(const R *__restrict__ vg, const int32_t *__restrict__ gidx, T *__restrict__ out, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (T)vg[gidx ? (int64_t)gidx[i] : i];
+}
+template <typename R>
+__global__ void k_scatter_v(const R *__restrict__ v, const int32_t *__restrict__ gidx, R *__restrict__ vg, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        vg[gidx ? (int64_t)gidx[i] : i] = v[i];
+}
+
+template <typename R, typename T>
+cudaError_t launch_gather_v(const R *vg, const int32_t *gidx, T *out, int64_t n, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    k_gather_v<R, T><<<grid_for(n, 256), 256, 0, st>>>(vg, gidx, out, n);
+    return cudaGetLastError();
+}
+template <typename R> cudaError_t launch_scatter_v(const R *v, const int32_t *gidx, R *vg, int64_t n, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    k_scatter_v<R><<<grid_for(n, 256), 256, 0, st>>>(v, gidx, vg, n);
+    return cudaGetLastError();
+}
+template cudaError_t launch_gather_v<float, float>(const float *, const int32_t *, float *, int64_t, cudaStream_t);
+template cudaError_t launch_gather_v<float, double>(const float *, const int32_t *, double *, int64_t, cudaStream_t);
+template cudaError_t launch_gather_v<double, float>(const double *, const int32_t *, float *, int64_t, cudaStream_t);
+template cudaError_t launch_gather_v<double, double>(const double *, const int32_t *, double *, int64_t, cudaStream_t);
+template cudaError_t launch_scatter_v<float>(const float *, const int32_t *, float *, int64_t, cudaStream_t);
+template cudaError_t launch_scatter_v<double>(const double *, const int32_t *, double *, int64_t, cudaStream_t);
+
+}  // namespace lqt

@@ -1,0 +1,146 @@
+"""Tissue simulations on the GPU (lqt_sim_*): 1D strands, 2D sheets, 3D volumes.
+
+`Sim` is the host-side handle of the drivers the reference writes as single
+`main()` programs (OneD.cc, new_11.cu, GPU3D.cu): geometry, stimulus protocol,
+stepping, V read-back, pseudo-ECG, activation / APD90 detectors, blow-up
+check and checkpoints.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+class Sim:
+    def __init__(self, types: np.ndarray, dx: float, *, fibre: np.ndarray | None = None, d_fibre: float = 0.154,
+                 d_trans: float = 0.0385, coeff_1d: np.ndarray | None = None, precision: int = N.MIXED,
+                 model: N.Model | str = "default", dt: float = 0.02, v0: float = -87.5, detect: bool = True,
+                 act_threshold: float = -30.0, vmin_ok: float = -200.0, vmax_ok: float = 200.0,
+                 stream: int | None = None):
+        t = np.ascontiguousarray(types, dtype=np.uint8)
+        self.shape = t.shape
+        dims = t.shape + (1,) * (3 - t.ndim)
+        self.types = t
+        self.dx = dx
+        f = None if fibre is None else np.ascontiguousarray(fibre, dtype=np.float32)
+        c1 = None if coeff_1d is None else np.ascontiguousarray(coeff_1d, dtype=np.float64)
+        self._keep = (t, f, c1)
+        geom = N.Geometry(dims[0], dims[1], dims[2], dx, _p(t), _p(f), d_fibre, d_trans, _p(c1))
+        m = N.model(model) if isinstance(model, str) else model
+        self.model = m
+        p = N.SimParams(dt, v0, precision, int(detect), m, act_threshold, vmin_ok, vmax_ok, C.c_void_p(stream or 0))
+        h = C.c_void_p()
+        N.check(N.lib().lqt_sim_create(C.byref(p), C.byref(geom), C.byref(h)), "lqt_sim_create")
+        self._h = h
+        self.n = int(N.lib().lqt_sim_num_tissue(h))
+        self.dt = dt
+        self.precision = precision
+        self.nel = 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib().lqt_sim_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    # ---- protocol ----------------------------------------------------------
+    def set_protocol(self, *, bcl: float, s1_mask: np.ndarray, s1_start: float = 0.0, s1_duration: float = 2.0,
+                     s1_strength: float = -52.0, s1_beats: int = 0, s1_onset: np.ndarray | None = None,
+                     s2_time: float = -1.0, s2_duration: float = 0.0, s2_strength: float = 0.0,
+                     s2_mask: np.ndarray | None = None):
+        m1 = np.ascontiguousarray(s1_mask, dtype=np.uint8).reshape(-1)
+        m2 = None if s2_mask is None else np.ascontiguousarray(s2_mask, dtype=np.uint8).reshape(-1)
+        on = None if s1_onset is None else np.ascontiguousarray(s1_onset, dtype=np.float32).reshape(-1)
+        q = N.Protocol(bcl, s1_start, s1_duration, s1_strength, s1_beats, 0, _p(m1), _p(on), s2_time, s2_duration,
+                       s2_strength, _p(m2))
+        N.check(N.lib().lqt_sim_set_protocol(self._h, C.byref(q)), "lqt_sim_set_protocol")
+
+    # ---- stepping ------------------------------------------------------------
+    def step(self, nsteps: int = 1):
+        N.check(N.lib().lqt_sim_step(self._h, int(nsteps)), "lqt_sim_step")
+
+    @property
+    def time(self) -> float:
+        return float(N.lib().lqt_sim_time(self._h))
+
+    # ---- read-back -------------------------------------------------------------
+    def get_v(self, as_double: bool = False) -> np.ndarray:
+        out = np.zeros(self.n, np.float64 if as_double else np.float32)
+        N.check(N.lib().lqt_sim_get_v(self._h, _p(out), int(as_double)), "lqt_sim_get_v")
+        return out
+
+    def get_v_into(self, out: np.ndarray):
+        """V into a caller buffer (float32 or float64, length n)."""
+        N.check(N.lib().lqt_sim_get_v(self._h, _p(out), int(out.dtype == np.float64)), "lqt_sim_get_v")
+
+    def tissue_index(self) -> np.ndarray:
+        out = np.zeros(self.n, np.int64)
+        N.check(N.lib().lqt_sim_tissue_index(self._h, _p(out)), "lqt_sim_tissue_index")
+        return out
+
+    def v_grid(self, fill=np.nan) -> np.ndarray:
+        g = np.full(self.types.size, fill, np.float32)
+        g[self.tissue_index()] = self.get_v()
+        return g.reshape(self.shape)
+
+    def get_state(self) -> np.ndarray:
+        s = np.zeros((self.n, N.NSTATE))
+        N.check(N.lib().lqt_sim_get_state(self._h, _p(s)), "lqt_sim_get_state")
+        return s
+
+    def set_state(self, s: np.ndarray):
+        s = np.ascontiguousarray(s, dtype=np.float64)
+        N.check(N.lib().lqt_sim_set_state(self._h, _p(s)), "lqt_sim_set_state")
+
+    def boundary(self):
+        L = N.lib()
+        L.lqt_sim_boundary.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]
+        n = C.c_int64()
+        N.check(L.lqt_sim_boundary(self._h, None, None, C.byref(n)), "lqt_sim_boundary")
+        d = np.zeros(n.value, np.int64)
+        s = np.zeros(n.value, np.int64)
+        N.check(L.lqt_sim_boundary(self._h, _p(d), _p(s), C.byref(n)), "lqt_sim_boundary")
+        return d, s
+
+    # ---- pseudo-ECG --------------------------------------------------------------
+    def set_electrodes(self, xyz, every: int = 50):
+        xyz = np.ascontiguousarray(np.asarray(xyz, np.float64).reshape(-1, 3))
+        self.nel = len(xyz)
+        N.check(N.lib().lqt_sim_set_electrodes(self._h, len(xyz), _p(xyz), every), "lqt_sim_set_electrodes")
+
+    def ecg(self):
+        n = C.c_int64()
+        N.check(N.lib().lqt_sim_get_ecg(self._h, 0, None, None, C.byref(n)), "lqt_sim_get_ecg")
+        phi = np.zeros((n.value, self.nel))
+        t = np.zeros(n.value)
+        N.check(N.lib().lqt_sim_get_ecg(self._h, n.value, _p(phi), _p(t), C.byref(n)), "lqt_sim_get_ecg")
+        return phi, t
+
+    # ---- detectors / checks -----------------------------------------------------------
+    def detect(self):
+        t_act = np.zeros(self.n, np.float32)
+        apd = np.zeros(self.n, np.float32)
+        ead = np.zeros(self.n, np.uint8)
+        N.check(N.lib().lqt_sim_get_detect(self._h, _p(t_act), _p(apd), _p(ead)), "lqt_sim_get_detect")
+        return dict(t_act=t_act, apd90=apd, ead=ead)
+
+    def check(self) -> int:
+        n = C.c_int64()
+        rc = N.lib().lqt_sim_check(self._h, C.byref(n))
+        if rc not in (N.OK, N.ERR_NUMERIC):
+            N.check(rc, "lqt_sim_check")
+        return int(n.value)
+
+    def checkpoint(self, path: str):
+        N.check(N.lib().lqt_sim_checkpoint(self._h, path.encode()), "lqt_sim_checkpoint")
+
+    def restore(self, path: str):
+        N.check(N.lib().lqt_sim_restore(self._h, path.encode()), "lqt_sim_restore")

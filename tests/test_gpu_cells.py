@@ -1,0 +1,82 @@
+"""GPU parity: the Cell interface (lqt_cells_*) against the CPU oracle."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lq():
+    import lqt1_gb300 as lq
+    lq.lib()
+    return lq
+
+
+def _random(orc, n, seed):
+    rng = np.random.default_rng(seed)
+    s = orc.random_states(n, seed=seed)
+    types = rng.integers(0, 5, n).astype(np.uint8)
+    ist = np.where(rng.random(n) < 0.2, -52.0, 0.0)
+    dg = rng.normal(0, 5, n)
+    return s, types, ist, dg
+
+
+@pytest.mark.parametrize("preset", ["default", "lqt1", "gpu3d"])
+def test_fp64_one_step_matches_oracle(lq, orc, preset):
+    """FP64 form, one TPORd::update() per cell: every state within 1e-9
+    relative (CUDA vs glibc exp/log differ in the last bits only)."""
+    n = 4096
+    s, types, ist, dg = _random(orc, n, 3)
+    ref = orc.cells_update(s.copy(), types, orc.model(preset), ist=ist, dvgap=dg, nsteps=1)
+    c = lq.TPORdCells(types, precision=lq.FP64, model=preset)
+    c.set_state(s)
+    c.set_istim(ist)
+    c.set_dvgap_dt(dg)
+    c.update(1)
+    got = c.get_state()
+    np.testing.assert_allclose(got, ref, rtol=1e-9, atol=1e-12)
+
+
+def test_fp64_many_steps_matches_oracle(lq, orc):
+    n = 2048
+    s, types, ist, dg = _random(orc, n, 5)
+    ref = orc.cells_update(s.copy(), types, orc.model("default"), ist=ist, dvgap=dg, nsteps=200)
+    c = lq.TPORdCells(types, precision=lq.FP64, model="default")
+    c.set_state(s)
+    c.set_istim(ist)
+    c.set_dvgap_dt(dg)
+    c.update(200)
+    got = c.get_state()
+    assert np.abs(got[:, 0] - ref[:, 0]).max() < 1e-6          # V, mV
+    np.testing.assert_allclose(got, ref, rtol=1e-6, atol=1e-9)
+
+
+def test_mixed_one_step_close_to_oracle(lq, orc):
+    """Mixed form (FP32 gates/currents, FP64 concentrations), one step."""
+    n = 4096
+    s, types, ist, dg = _random(orc, n, 9)
+    ref = orc.cells_update(s.copy(), types, orc.model("default"), ist=ist, dvgap=dg, nsteps=1)
+    c = lq.TPORdCells(types, precision=lq.MIXED, model="default")
+    c.set_state(s)
+    c.set_istim(ist)
+    c.set_dvgap_dt(dg)
+    c.update(1)
+    got = c.get_state()
+    assert np.abs(got[:, 0] - ref[:, 0]).max() < 2e-3           # mV
+    assert np.abs(got[:, 9:37] - ref[:, 9:37]).max() < 1e-4     # gates
+    np.testing.assert_allclose(got[:, 1:9], ref[:, 1:9], rtol=1e-6)
+
+
+def test_state_roundtrip_and_dump(lq, orc, tmp_path):
+    s, types, _, _ = _random(orc, 64, 1)
+    for prec in (lq.FP64, lq.MIXED):
+        c = lq.TPORdCells(types, precision=prec)
+        c.set_state(s)
+        got = c.get_state()
+        if prec == lq.FP64:
+            assert np.array_equal(got, s)
+        else:
+            np.testing.assert_allclose(got, s, rtol=1e-7)
+        c.output_all_states(str(tmp_path / "st.dat"), 3)
+        lines = open(tmp_path / "st.dat").read().split()
+        assert len(lines) == 40
