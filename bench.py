@@ -1,0 +1,333 @@
+"""Benchmark of the monodomain TPORd step on the 3D ventricle-shaped workload.
+
+One "step" advances every tissue voxel of the workload by dt = 0.02 ms:
+stimulus + anisotropic diffusion + TPORd ionic update + V update +
+activation / APD90 detectors, with the pseudo-ECG of 6 electrodes sampled
+every 50 steps.  The metric is cell-steps/s (voxels x steps / s).
+
+Default: 3D truncated prolate-ellipsoid shell in a 320x320x420 grid at
+0.2 mm (about 7.1M tissue voxels), fibres +60 -> -60 degrees, IKs x0.5,
+beta-adrenergic ICaL x2 / IKs x1.5, apical stimulus at BCL 800 ms; the mixed
+form (FP32 gates/currents/diffusion, FP64 concentrations).  The plain FP64
+form is timed on the same state and reported beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload ventricle3d|sheet2d]
+
+Under torchrun each rank runs an independent replica (the path has no data
+exchange between instances); value = voxel-steps of all ranks / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "monodomain cell-steps/s: plain FP64 vs FP32/surrogate form at ≤1 ms APD90 err"
+UNIT = "cell-steps/s"
+# algorithmic bytes per voxel-step of the fused step kernel (k_grid_step):
+# state read+write (8 FP64 concentrations, 29 evolving gates/fluxes), own V
+# read + write, tissue->grid index, control byte, diffusion tensor (6) and its
+# divergence (3), AP-detector record (16 B read)
+BYTES_MIXED = 8 * 8 * 2 + 29 * 4 * 2 + 4 + 4 + 4 + 1 + 9 * 4 + 16
+BYTES_FP64 = 8 * 8 * 2 + 29 * 8 * 2 + 8 + 8 + 4 + 1 + 9 * 8 + 16
+
+
+def workload_model():
+    import lqt1_gb300 as lq
+    # IKs x0.5 (LQT1), beta-adrenergic ICaL x2 / IKs x1.5, no gate shifts
+    return lq.model("baseline", gks_scale=0.5, pca_scale=2.0, gks_iso_scale=1.5)
+
+
+def build_workload(name):
+    import lqt1_gb300 as lq
+    if name in ("ventricle3d", "ventricle3d_small"):
+        v = lq.geometry.ventricle() if name == "ventricle3d" else lq.geometry.ventricle(
+            nx=170, ny=170, nz=220, a_out=14.0, c_out=36.0, wall=6.0, z_base=40.0, island_radius=4.0,
+            stim_radius=2.0)
+        # six electrodes around the mid-height, 20 mm outside the epicardium
+        cx, cy = v.spec.cx, v.spec.cy
+        zm = v.spec.z_base - 0.5 * v.spec.c_out
+        r = v.spec.a_out + 20.0
+        el = [(cx + r * math.cos(a), cy + r * math.sin(a), zm) for a in np.linspace(0, 2 * math.pi, 7)[:-1]]
+        nt = int((v.types != 255).sum())
+        return dict(types=v.types, fibre=v.fibre, s1=v.s1_mask, dx=0.2, bcl=800.0, electrodes=el,
+                    desc="3d-ventricle %dx%dx%d @0.2mm, %d tissue voxels" % (v.types.shape + (nt,)))
+    sh = lq.geometry.sheet(600, 600)
+    return dict(types=sh.types, fibre=None, s1=sh.s1_mask, s2=sh.s2_mask, dx=0.15, bcl=1000.0,
+                electrodes=[(45.0, 45.0, 10.0)], desc="2d-sheet 600x600 @0.15mm")
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{device}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [r.split(", ") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        except OSError:
+            return None
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = max(float(r[2]) for r in rows if r[2].replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 5 + i and r[5 + i].strip() == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+def traffic_summary():
+    """Per-launch DRAM bytes of k_grid_step from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "k_grid_step_ventricle3d.json")
+    try:
+        d = json.load(open(p))
+        return d.get("traffic_bytes_per_launch_full_workload")
+    except (OSError, ValueError):
+        return None
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(w, max_voxels=200_000):
+    """A bounded sample of the workload for the CPU oracle: a slab of the grid
+    (full y, z; a range of x planes) with ~max_voxels tissue voxels, its faces
+    emptied so the oracle grid is valid."""
+    t = w["types"]
+    per_x = (t != 255).reshape(t.shape[0], -1).sum(1)
+    x0 = int(np.argmax(per_x > 0))
+    x1 = x0
+    tot = 0
+    while x1 < t.shape[0] and tot < max_voxels:
+        tot += per_x[x1]
+        x1 += 1
+    sl = slice(max(0, x0 - 1), min(t.shape[0], x1 + 1))
+    sub = t[sl].copy()
+    sub[0] = 255
+    sub[-1] = 255
+    fib = None if w["fibre"] is None else np.ascontiguousarray(w["fibre"][sl])
+    return sub, fib
+
+
+def run_cpu(w, steps, warmup, seconds=None):
+    from oracle import orc
+    orc.build()
+    sub, fib = cpu_sample(w)
+    og = orc.Grid(sub, w["dx"], fibre=fib)
+    m = orc.model(dict(dss_shift=0, fss_shift=0, pca_scale=2.0, gks_scale=0.5, gks_iso_scale=1.5, suprep_dose=0))
+    st = orc.initial_state(-87.5, og.n)
+    cores = os.cpu_count() or 1
+    for _ in range(warmup):
+        og.step(st, m, 0.02, None, cores)
+    t0 = time.perf_counter()
+    done = 0
+    while done < steps and (seconds is None or time.perf_counter() - t0 < seconds or done < 3):
+        og.step(st, m, 0.02, None, cores)
+        done += 1
+    el = time.perf_counter() - t0
+    return dict(value=og.n * done / el, cores=cores, n=og.n, steps=done, seconds=el)
+
+
+def cpu_model_name():
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="ventricle3d", choices=["ventricle3d", "ventricle3d_small", "sheet2d"])
+    ap.add_argument("--prerun", type=int, default=1000, help="untimed steps to start the wave (setup)")
+    ap.add_argument("--fp64-steps", type=int, default=10)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        w = build_workload(args.workload)
+        r = run_cpu(w, args.steps, args.warmup, seconds=60.0)
+        cb = {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": "port",
+              "sample": f"{r['n']} tissue voxels of the workload (x-slab), {r['steps']} steps, oracle FP64 "
+                        f"restatement of TPORd.cc + 3D diffusion, OpenMP, {cpu_model_name()}"}
+        line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": r["steps"],
+                "warmup": args.warmup, "ms_per_step": 1e3 * r["seconds"] / r["steps"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": w["desc"] + " (CPU sample)", "l2": "n/a (CPU)"}, "impl": "reference",
+                "cpu_baseline": cb, "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                                            "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+    import lqt1_gb300 as lq
+
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.cuda.current_device()
+    w = build_workload(args.workload)
+    stream = torch.cuda.Stream()
+    sim = lq.Sim(w["types"], w["dx"], fibre=w["fibre"], precision=lq.MIXED, model=workload_model(), detect=True,
+                 vmin_ok=-200.0, vmax_ok=200.0, stream=stream.cuda_stream)
+    sim.set_protocol(bcl=w["bcl"], s1_mask=w["s1"], s1_start=0.0, s1_duration=2.0, s1_strength=-52.0, s1_beats=3,
+                     s2_time=-1.0)
+    sim.set_electrodes(np.array(w["electrodes"]), every=50)
+    n = sim.n
+    sim.step(args.prerun)
+    sim.step(args.warmup)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        sim.step(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n * args.steps / (ms / 1e3)
+    nbad = sim.check()
+
+    # roofline of the dominant kernel: per-launch CUDA-event time of k_grid_step
+    ms_step, ms_ghost = sim.profile(20)
+    peaks = measured_peaks()
+    peak = peaks.get("hbm_gbs")
+    peak_kind = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    achieved = BYTES_MIXED * n / (ms_step / 1e3) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic_summary(), "kernel": "k_grid_step<float,3>", "kernel_ms": ms_step,
+            "bytes_per_cell_step": BYTES_MIXED, "peak_source": peak_kind}
+
+    # e2e through the C ABI with pinned host buffers: initial state H2D, then
+    # every step lqt_sim_step + lqt_sim_get_v (the reference's host loop
+    # copies V back every step, GPU3D.cu:1802), final state D2H.
+    st_host = torch.empty((n, 40), dtype=torch.float64, pin_memory=True).numpy()
+    v_host = torch.empty(n, dtype=torch.float32, pin_memory=True).numpy()
+    sim.get_state(out=st_host)
+    k_e2e = max(10, min(args.steps, 200))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim.set_state(st_host)
+    for _ in range(k_e2e):
+        sim.step(1)
+        sim.get_v_into(v_host)
+    sim.get_state(out=st_host)
+    t_e2e = time.perf_counter() - t0
+    e2e = {"value": world * n * k_e2e / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(n * 320 / k_e2e),
+           "d2h_bytes_per_step": int(n * 4 + n * 320 / k_e2e), "steps": k_e2e}
+
+    # plain FP64 form on the same state
+    fp64 = None
+    if args.fp64_steps > 0:
+        s64 = lq.Sim(w["types"], w["dx"], fibre=w["fibre"], precision=lq.FP64, model=workload_model(), detect=True,
+                     stream=stream.cuda_stream)
+        s64.set_protocol(bcl=w["bcl"], s1_mask=w["s1"], s1_start=0.0, s1_duration=2.0, s1_strength=-52.0,
+                         s1_beats=3)
+        s64.set_state(st_host)
+        s64.step(2)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        s64.step(args.fp64_steps)
+        b.record(stream)
+        torch.cuda.synchronize()
+        v64 = n * args.fp64_steps / (a.elapsed_time(b) / 1e3)
+        ms64, _ = s64.profile(2)
+        fp64 = {"value": v64 * world, "unit": UNIT, "steps": args.fp64_steps, "kernel_ms": ms64,
+                "achieved_gbs": BYTES_FP64 * n / (ms64 / 1e3) / 1e9, "mixed_over_fp64": value / (v64 * world)}
+        s64.close()
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        r = run_cpu(w, 10_000, 1, seconds=15.0)
+        cpu = {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": "port",
+               "sample": f"{r['n']} tissue voxels (x-slab of the workload), {r['steps']} steps, FP64 oracle, "
+                         f"OpenMP on {r['cores']} threads, {cpu_model_name()}"}
+    clocks = clk.summary()
+    ecg_launches = 2 * (args.steps // 50)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": w["desc"], "tissue_voxels": n, "form": "mixed (FP32 gates/currents/diffusion, "
+                       "FP64 concentrations)", "dt_ms": 0.02, "electrodes": len(w["electrodes"]),
+                       "l2": "inputs larger than L2 (state %.2f GB/step)" % (BYTES_MIXED * n / 1e9),
+                       "parallelism": f"replicas x{world}"},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "fp64_form": fp64,
+            "gpu_launches": 2 * args.steps + ecg_launches, "clocks": clocks, "blowup_voxel_steps": nbad}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -230,6 +230,8 @@ typedef struct lqt_protocol {
     const uint8_t *s2_mask;    /* nx*ny*nz host array: 1 = receives S2 */
 } lqt_protocol;
 
+/* A NULL stream makes the simulation create and own a non-blocking stream
+ * (graph capture cannot use the legacy default stream). */
 typedef struct lqt_sim_params {
     double dt;                 /* ms (0.02 in every reference driver) */
     double v0;                 /* initial V, mV */
@@ -279,6 +281,12 @@ int lqt_sim_get_ecg(lqt_sim *s, int64_t max_samples, double *phi_host,
  * 90% repolarisation).  NULL pointers are skipped. */
 int lqt_sim_get_detect(lqt_sim *s, float *t_act_host, float *apd90_host,
                        uint8_t *ead_host);
+
+/* Instrumentation (no counterpart in the reference, which has no timing):
+ * run nsteps steps without graph capture, timing each launch of the fused
+ * step kernel and of the ghost/clock kernel with CUDA events on the
+ * simulation's stream; returns the mean milliseconds per launch. */
+int lqt_sim_profile(lqt_sim *s, int64_t nsteps, double *ms_step, double *ms_ghost);
 
 /* Mirror-boundary map (GPU3D.cu:1487-1604): the empty grid voxels next to
  * tissue and, for each, the grid index of the tissue voxel whose V it holds.

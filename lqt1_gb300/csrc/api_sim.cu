@@ -694,6 +694,46 @@ int lqt_sim_get_detect(lqt_sim *s, float *t_act, float *apd90, uint8_t *ead)
     return LQT_OK;
 }
 
+int lqt_sim_profile(lqt_sim *s, int64_t nsteps, double *ms_step, double *ms_ghost)
+{
+    if (!s || nsteps <= 0) return fail(LQT_ERR_INVALID, "lqt_sim_profile: NULL handle or nsteps <= 0");
+    cudaEvent_t ev[3];
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    double t_step = 0, t_ghost = 0;
+    const StepK k = make_stepk(s->p.dt);
+    int rc = LQT_OK;
+    for (int64_t i = 0; i < nsteps && rc == LQT_OK; ++i) {
+        cudaError_t e = cudaEventRecord(ev[0], s->stream);
+        if (s->fp64()) {
+            const GridDev<double> g = devf<double>(s);
+            if (e == cudaSuccess) e = launch_grid_step<double>(g, k, s->cur, s->dim, s->stream);
+            if (e == cudaSuccess) e = cudaEventRecord(ev[1], s->stream);
+            if (e == cudaSuccess) e = launch_ghost<double>(g, s->cur ^ 1, s->stream);
+        } else {
+            const GridDev<float> g = devf<float>(s);
+            if (e == cudaSuccess) e = launch_grid_step<float>(g, k, s->cur, s->dim, s->stream);
+            if (e == cudaSuccess) e = cudaEventRecord(ev[1], s->stream);
+            if (e == cudaSuccess) e = launch_ghost<float>(g, s->cur ^ 1, s->stream);
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(ev[2], s->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev[2]);
+        float a = 0, b = 0;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&a, ev[0], ev[1]);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&b, ev[1], ev[2]);
+        if (e != cudaSuccess) rc = fail(LQT_ERR_CUDA, std::string("lqt_sim_profile: ") + cudaGetErrorString(e));
+        t_step += a;
+        t_ghost += b;
+        s->cur ^= 1;
+        s->step += 1;
+        s->time += s->p.dt;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    if (rc) return rc;
+    if (ms_step) *ms_step = t_step / nsteps;
+    if (ms_ghost) *ms_ghost = t_ghost / nsteps;
+    return LQT_OK;
+}
+
 int lqt_sim_boundary(const lqt_sim *s, int64_t *dst, int64_t *src, int64_t *n)
 {
     if (!s || !n) return fail(LQT_ERR_INVALID, "lqt_sim_boundary: NULL");

@@ -91,14 +91,24 @@ class Sim:
         g[self.tissue_index()] = self.get_v()
         return g.reshape(self.shape)
 
-    def get_state(self) -> np.ndarray:
-        s = np.zeros((self.n, N.NSTATE))
+    def get_state(self, out: np.ndarray | None = None) -> np.ndarray:
+        s = np.zeros((self.n, N.NSTATE)) if out is None else out
+        assert s.dtype == np.float64 and s.flags.c_contiguous and s.size == self.n * N.NSTATE
         N.check(N.lib().lqt_sim_get_state(self._h, _p(s)), "lqt_sim_get_state")
         return s
 
     def set_state(self, s: np.ndarray):
         s = np.ascontiguousarray(s, dtype=np.float64)
         N.check(N.lib().lqt_sim_set_state(self._h, _p(s)), "lqt_sim_set_state")
+
+    def profile(self, nsteps: int = 20):
+        """Mean device ms per launch of the fused step kernel and of the ghost
+        kernel (CUDA events on the simulation's stream)."""
+        L = N.lib()
+        L.lqt_sim_profile.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        a, b = C.c_double(), C.c_double()
+        N.check(L.lqt_sim_profile(self._h, int(nsteps), C.byref(a), C.byref(b)), "lqt_sim_profile")
+        return a.value, b.value
 
     def boundary(self):
         L = N.lib()
