@@ -68,6 +68,7 @@ struct lqt_batch {
         b.max_beats = p.max_beats;
         b.win = win;
         b.models = models;
+        b.dt = p.dt;
         b.queue = queue;
         b.nbad = nbad;
         b.vmin_ok = -200.0;

@@ -97,12 +97,12 @@ struct lqt_sim {
         g.sy = dim == 2 ? 1 : nz;
         g.pad = 0;
         g.dx = dx;
-        g.inv_dx = 1.0 / dx;
-        g.inv_2dx = 1.0 / (2.0 * dx);
-        g.inv_dx2 = 1.0 / (dx * dx);
-        g.inv_4dx2 = 1.0 / (4.0 * dx * dx);
+        g.inv_dx = (R)(1.0 / dx);
+        g.inv_2dx = (R)(1.0 / (2.0 * dx));
+        g.inv_dx2 = (R)(1.0 / (dx * dx));
+        g.inv_4dx2 = (R)(1.0 / (4.0 * dx * dx));
         g.dt = p.dt;
-        g.model = make_modelk(p.model);
+        g.model = model_as<R>(make_modelk(p.model));
         g.clk = clk;
         g.win = win;
         g.nwin = nwin;
@@ -111,16 +111,16 @@ struct lqt_sim {
         g.bcl = has_protocol ? proto.bcl : 1.0;
         g.s1_start = proto.s1_start;
         g.s1_dur = proto.s1_duration;
-        g.s1_strength = proto.s1_strength;
-        g.s2_strength = proto.s2_strength;
+        g.s1_strength = (R)proto.s1_strength;
+        g.s2_strength = (R)proto.s2_strength;
         g.onset = onset;
         g.bnd_dst = bnd_dst;
         g.bnd_src = bnd_src;
         g.det = det;
         g.apd90 = apd90;
         g.act_thr = (float)p.act_threshold;
-        g.vmin_ok = p.vmin_ok;
-        g.vmax_ok = p.vmax_ok;
+        g.vmin_ok = (R)p.vmin_ok;
+        g.vmax_ok = (R)p.vmax_ok;
         g.nbad = nbad;
         return g;
     }
@@ -132,7 +132,7 @@ namespace {
 template <typename R> GridDev<R> devf(const lqt_sim *s)
 {
     GridDev<R> g = s->dev<R>();
-    g.diso = s->diso;
+    g.diso = (R)s->diso;
     return g;
 }
 
@@ -182,6 +182,7 @@ int refresh_windows(lqt_sim *s, int64_t horizon)
     Clock c{};
     c.step = s->step;
     c.time = s->time;
+    c.time_f = (float)s->time;
     int32_t wi = 0;
     while (wi < s->nwin && s->step >= w[wi].off) ++wi;
     c.widx = wi;
@@ -621,6 +622,7 @@ int lqt_sim_set_state(lqt_sim *s, const double *state_host)
     Clock c{};
     c.step = s->step;
     c.time = s->time;
+    c.time_f = (float)s->time;
     c.s1_cycle_ok = 1;
     CK(cudaMemcpy(s->clk, &c, sizeof(c), cudaMemcpyHostToDevice));
     return LQT_OK;

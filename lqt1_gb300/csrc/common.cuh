@@ -4,7 +4,9 @@
 // multiple of 128 cells so every array starts 512-byte aligned):
 //   v      R     [ld]        membrane potential (cells and strands; grids keep
 //                            V in a dense double-buffered grid instead)
-//   conc   double[8][ld]     nai nass ki kss cai cass cansr cajsr
+//   conc   double[8][ld]     nai nass ki kss cai cass cansr cajsr (FP64 form);
+//          float[16][ld]     the mixed form's Kahan pairs in the same bytes:
+//                            hi parts [0..8), lo parts [8..16)
 //   gate   R     [31][ld]    reference state indices 9..39 (sm .. CaMKt);
 //                            slots 3, 4 (hsp, jp) are constant and not touched
 // R = double for the FP64 form, float for the mixed form.
@@ -22,16 +24,39 @@ namespace lqt {
 template <typename T> __device__ __forceinline__ T ld_stream(const T *p) { return __ldcs(p); }
 template <typename T> __device__ __forceinline__ void st_stream(T *p, T v) { __stcs(p, v); }
 
+__device__ __forceinline__ void load_conc(double *dst[8], const double *conc, int64_t ld, int64_t i)
+{
+#pragma unroll
+    for (int j = 0; j < 8; ++j) *dst[j] = ld_stream(conc + j * ld + i);
+}
+__device__ __forceinline__ void load_conc(float2 *dst[8], const double *conc, int64_t ld, int64_t i)
+{
+    const float *f = reinterpret_cast<const float *>(conc);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) *dst[j] = make_float2(ld_stream(f + j * ld + i), ld_stream(f + (8 + j) * ld + i));
+}
+__device__ __forceinline__ void store_conc(double *const src[8], double *conc, int64_t ld, int64_t i)
+{
+#pragma unroll
+    for (int j = 0; j < 8; ++j) st_stream(conc + j * ld + i, *src[j]);
+}
+__device__ __forceinline__ void store_conc(float2 *const src[8], double *conc, int64_t ld, int64_t i)
+{
+    float *f = reinterpret_cast<float *>(conc);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        st_stream(f + j * ld + i, src[j]->x);
+        st_stream(f + (8 + j) * ld + i, src[j]->y);
+    }
+}
+
 template <typename R>
 __device__ __forceinline__ void load_cell(CellState<R> &c, const SoA<R> &s, int64_t i)
 {
     const int64_t ld = s.ld;
-    const double *C = s.conc + i;
     const R *G = s.gate + i;
-    c.nai = ld_stream(C + 0 * ld); c.nass = ld_stream(C + 1 * ld);
-    c.ki = ld_stream(C + 2 * ld); c.kss = ld_stream(C + 3 * ld);
-    c.cai = ld_stream(C + 4 * ld); c.cass = ld_stream(C + 5 * ld);
-    c.cansr = ld_stream(C + 6 * ld); c.cajsr = ld_stream(C + 7 * ld);
+    typename CellState<R>::C *cp[8] = {&c.nai, &c.nass, &c.ki, &c.kss, &c.cai, &c.cass, &c.cansr, &c.cajsr};
+    load_conc(cp, s.conc, ld, i);
     c.sm = ld_stream(G + 0 * ld); c.sh = ld_stream(G + 1 * ld); c.sj = ld_stream(G + 2 * ld);
     c.mL = ld_stream(G + 5 * ld); c.hL = ld_stream(G + 6 * ld); c.hLp = ld_stream(G + 7 * ld);
     c.a = ld_stream(G + 8 * ld); c.iF = ld_stream(G + 9 * ld); c.iS = ld_stream(G + 10 * ld);
@@ -48,12 +73,10 @@ template <typename R>
 __device__ __forceinline__ void store_cell(const CellState<R> &c, const SoA<R> &s, int64_t i)
 {
     const int64_t ld = s.ld;
-    double *C = s.conc + i;
     R *G = s.gate + i;
-    st_stream(C + 0 * ld, c.nai); st_stream(C + 1 * ld, c.nass);
-    st_stream(C + 2 * ld, c.ki); st_stream(C + 3 * ld, c.kss);
-    st_stream(C + 4 * ld, c.cai); st_stream(C + 5 * ld, c.cass);
-    st_stream(C + 6 * ld, c.cansr); st_stream(C + 7 * ld, c.cajsr);
+    CellState<R> &cc = const_cast<CellState<R> &>(c);
+    typename CellState<R>::C *cp[8] = {&cc.nai, &cc.nass, &cc.ki, &cc.kss, &cc.cai, &cc.cass, &cc.cansr, &cc.cajsr};
+    store_conc(cp, s.conc, ld, i);
     st_stream(G + 0 * ld, c.sm); st_stream(G + 1 * ld, c.sh); st_stream(G + 2 * ld, c.sj);
     st_stream(G + 5 * ld, c.mL); st_stream(G + 6 * ld, c.hL); st_stream(G + 7 * ld, c.hLp);
     st_stream(G + 8 * ld, c.a); st_stream(G + 9 * ld, c.iF); st_stream(G + 10 * ld, c.iS);

@@ -17,6 +17,7 @@ constexpr int kMaxElectrodes = 8;
 struct Clock {
     int64_t step;
     double time;        // accumulated as `time += dt` (OneD.cc:317)
+    float time_f;       // the same, rounded once for the detectors
     double tb;          // time - floor(time/bcl)*bcl (only kept with onsets)
     int32_t widx;       // current S1 window
     int32_t s1_on, s2_on, opened, s1_cycle_ok, pad;
@@ -29,26 +30,27 @@ template <typename R> struct GridDev {
     const uint8_t *ctl;            // type + stimulus bits
     const R *d6, *b3;              // anisotropic tensor and its divergence, or null
     const R *coeff, *dcoeff;       // 1D: D and dD/dx per cell
-    double diso;                   // isotropic D
+    R diso;                        // isotropic D
     int64_t ntissue, nbnd;
     int64_t sx, sy;                // dense strides of x and y (z stride 1)
     int64_t pad;                   // grid origin offset (0)
-    double dx, inv_dx, inv_2dx, inv_dx2, inv_4dx2;
+    double dx;
+    R inv_dx, inv_2dx, inv_dx2, inv_4dx2;
     double dt;
-    ModelK model;
+    ModelT<R> model;
     Clock *clk;
     const Win *win;                // S1 windows
     int32_t nwin;
     int32_t s1_beats;
     Win s2_win;
     double bcl, s1_start, s1_dur;
-    double s1_strength, s2_strength;
+    R s1_strength, s2_strength;
     const float *onset;            // per tissue voxel onset delay, or null
     const int32_t *bnd_dst, *bnd_src;
     float4 *det;                   // {vrest, vpeak, t_act, bits}, or null
     float *apd90;
     float act_thr;
-    double vmin_ok, vmax_ok;
+    R vmin_ok, vmax_ok;
     unsigned long long *nbad;
 };
 

@@ -28,29 +28,29 @@ __global__ void __launch_bounds__(128) k_cells_update(SoA<R> s, const uint8_t *_
                                                       const double *__restrict__ ist,
                                                       const double *__restrict__ dvgap, double *__restrict__ dvdt,
                                                       const ModelK *__restrict__ models,
-                                                      const uint16_t *__restrict__ model_of, StepK k, int64_t n,
+                                                      const uint16_t *__restrict__ model_of, StepT<R> k, int64_t n,
                                                       int64_t nsteps)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         CellState<R> c;
         load_cell(c, s, i);
         c.v = s.v[i];
-        const ModelK m = models[model_of ? model_of[i] : 0];
+        const ModelT<R> m = model_as<R>(models[model_of ? model_of[i] : 0]);
         const R is = ist ? (R)ist[i] : (R)0;
         const R dg = dvgap ? (R)dvgap[i] : (R)0;
         const int ct = ctype[i];
-        StepOut o{0.0};
+        StepOut<R> o{};
         for (int64_t t = 0; t < nsteps; ++t) tpord_step<R>(c, ct, m, k, is, dg, &o);
         store_cell(c, s, i);
         s.v[i] = c.v;
-        if (dvdt) dvdt[i] = o.dvdt;
+        if (dvdt) dvdt[i] = (double)o.dvdt;
     }
 }
 
 // ------------------------------------------------------------------------
 // Persistent batch kernel.
 template <typename R, int MAXT>
-__global__ void __launch_bounds__(MAXT) k_batch(BatchDev<R> b, StepK k)
+__global__ void __launch_bounds__(MAXT) k_batch(BatchDev<R> b, StepT<R> k)
 {
     __shared__ R vbuf[2][MAXT];
     __shared__ double red[MAXT / 32];
@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(MAXT) k_batch(BatchDev<R> b, StepK k)
         CellState<R> c{};
         int ct = 3;
         R coeff = 0, dcoeff = 0;
-        ModelK m{};
+        ModelT<R> m{};
         if (active) {
             seg = b.segs[b.seg_of[cell]];
             li = (int)(cell - seg.cell0);
@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(MAXT) k_batch(BatchDev<R> b, StepK k)
             ct = b.ctype[cell];
             coeff = b.coeff ? (R)b.coeff[cell] : (R)0;
             dcoeff = b.dcoeff ? (R)b.dcoeff[cell] : (R)0;
-            m = b.models[seg.model];
+            m = model_as<R>(b.models[seg.model]);
         }
         // stimulus windows: [on, off) step ranges, host-computed from the
         // reference's floating `time += dt` (OneD.cc:317,337-338)
@@ -100,6 +100,7 @@ __global__ void __launch_bounds__(MAXT) k_batch(BatchDev<R> b, StepK k)
         const bool strand = seg.n > 1;
         const R dx = (R)seg.dx;
         const R inv_dx = (R)1 / dx, inv_2dx = (R)1 / ((R)2 * dx), inv_dx2 = (R)1 / (dx * dx);
+        const R stim = (R)seg.stim;
         double time = 0.0;
         int cur = 0;
         vbuf[0][t] = active ? c.v : (R)0;
@@ -160,12 +161,12 @@ __global__ void __launch_bounds__(MAXT) k_batch(BatchDev<R> b, StepK k)
                 }
                 if (st == w_on) opened = true;
                 const bool on = st >= w_on && st < w_off && li < seg.n_stim;
-                const R ist = on ? (R)seg.stim : (R)0;
+                const R ist = on ? stim : (R)0;
                 if (opened && b.det_t_act) {
                     det_open_cycle(det, (float)vo);
                     ++beat;
                 }
-                StepOut o{0.0};
+                StepOut<R> o{};
                 tpord_step<R>(c, ct, m, k, ist, dvgap, &o);
                 vbuf[cur ^ 1][t] = c.v;
 
@@ -195,7 +196,7 @@ __global__ void __launch_bounds__(MAXT) k_batch(BatchDev<R> b, StepK k)
             } else if (active) {
                 vbuf[cur ^ 1][t] = vbuf[cur][t];
             }
-            time += k.dt;
+            time += b.dt;
             cur ^= 1;
         }
         // ECG of the final recorded step
@@ -239,7 +240,8 @@ cudaError_t launch_cells_update(const SoA<R> &s, const uint8_t *ctype, const dou
     const int bs = 128;
     int64_t nb = (n + bs - 1) / bs;
     if (nb > 152 * 64) nb = 152 * 64;
-    k_cells_update<R><<<(unsigned)nb, bs, 0, stream>>>(s, ctype, ist, dvgap, dvdt, models, model_of, k, n, nsteps);
+    k_cells_update<R><<<(unsigned)nb, bs, 0, stream>>>(s, ctype, ist, dvgap, dvdt, models, model_of, step_as<R>(k), n,
+                                                       nsteps);
     return cudaGetLastError();
 }
 
@@ -248,11 +250,11 @@ cudaError_t launch_batch(const BatchDev<R> &b, const StepK &k, int threads, int 
 {
     if (b.nitems <= 0) return cudaSuccess;
     if (threads <= 128)
-        k_batch<R, 128><<<ctas, 128, 0, stream>>>(b, k);
+        k_batch<R, 128><<<ctas, 128, 0, stream>>>(b, step_as<R>(k));
     else if (threads <= 256)
-        k_batch<R, 256><<<ctas, 256, 0, stream>>>(b, k);
+        k_batch<R, 256><<<ctas, 256, 0, stream>>>(b, step_as<R>(k));
     else
-        k_batch<R, 512><<<ctas, 512, 0, stream>>>(b, k);
+        k_batch<R, 512><<<ctas, 512, 0, stream>>>(b, step_as<R>(k));
     return cudaGetLastError();
 }
 

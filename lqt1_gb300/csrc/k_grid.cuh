@@ -32,22 +32,22 @@ __device__ __forceinline__ R grid_du(const GridDev<R> &gd, const R *__restrict__
         if (n == 1) return (R)0;
         if (g == 0) {
             const R vp = V[g + 1];
-            fo = (vp - vc) * (R)gd.inv_dx;
-            so = (vp + vc - (R)2 * vc) * (R)gd.inv_dx2;
+            fo = (vp - vc) * gd.inv_dx;
+            so = (vp + vc - (R)2 * vc) * gd.inv_dx2;
         } else if (g == n - 1) {
             const R vm = V[g - 1];
-            fo = (vc - vm) * (R)gd.inv_dx;
-            so = (vc + vm - (R)2 * vc) * (R)gd.inv_dx2;
+            fo = (vc - vm) * gd.inv_dx;
+            so = (vc + vm - (R)2 * vc) * gd.inv_dx2;
         } else {
             const R vp = V[g + 1], vm = V[g - 1];
-            fo = (vp - vm) * (R)gd.inv_2dx;
-            so = (vp + vm - (R)2 * vc) * (R)gd.inv_dx2;
+            fo = (vp - vm) * gd.inv_2dx;
+            so = (vp + vm - (R)2 * vc) * gd.inv_dx2;
         }
         return (R)gd.dcoeff[k] * fo + (R)gd.coeff[k] * so;
     } else {
         const int64_t sx = gd.sx, sy = gd.sy;
         const R vxp = V[g + sx], vxm = V[g - sx], vyp = V[g + sy], vym = V[g - sy];
-        const R c2 = (R)gd.inv_dx2;
+        const R c2 = gd.inv_dx2;
         const R lxx = (vxp + vxm - (R)2 * vc) * c2;
         const R lyy = (vyp + vym - (R)2 * vc) * c2;
         R lzz = 0, vzp = 0, vzm = 0;
@@ -56,10 +56,10 @@ __device__ __forceinline__ R grid_du(const GridDev<R> &gd, const R *__restrict__
             vzm = V[g - 1];
             lzz = (vzp + vzm - (R)2 * vc) * c2;
         }
-        if (!gd.d6) return (R)gd.diso * (lxx + lyy + lzz);
+        if (!gd.d6) return gd.diso * (lxx + lyy + lzz);
         const R *D = gd.d6 + 6 * k;
         const R *B = gd.b3 + 3 * k;
-        const R c4 = (R)gd.inv_4dx2, c1 = (R)gd.inv_2dx;
+        const R c4 = gd.inv_4dx2, c1 = gd.inv_2dx;
         const R lxy = (V[g + sx + sy] + V[g - sx - sy] - V[g - sx + sy] - V[g + sx - sy]) * c4;
         R du = D[0] * lxx + D[1] * lyy + (R)2 * D[3] * lxy + B[0] * ((vxp - vxm) * c1) + B[1] * ((vyp - vym) * c1);
         if constexpr (DIM == 3) {
@@ -72,7 +72,7 @@ __device__ __forceinline__ R grid_du(const GridDev<R> &gd, const R *__restrict__
 }
 
 template <typename R, int DIM>
-__global__ void __launch_bounds__(256) k_grid_step(GridDev<R> gd, StepK kst, int cur)
+__global__ void __launch_bounds__(256) k_grid_step(GridDev<R> gd, StepT<R> kst, int cur)
 {
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k >= gd.ntissue) return;
@@ -88,16 +88,16 @@ __global__ void __launch_bounds__(256) k_grid_step(GridDev<R> gd, StepK kst, int
     if (gd.onset) {
         // per-voxel onset within each cycle (GPU3D.cu:397-409)
         const double on = gd.s1_start + (double)gd.onset[k];
-        if ((ctl & kCtlS1) && ck.s1_cycle_ok && ck.tb >= on && ck.tb < on + gd.s1_dur) ist = (R)gd.s1_strength;
+        if ((ctl & kCtlS1) && ck.s1_cycle_ok && ck.tb >= on && ck.tb < on + gd.s1_dur) ist = gd.s1_strength;
     } else if (ck.s1_on && (ctl & kCtlS1)) {
-        ist = (R)gd.s1_strength;
+        ist = gd.s1_strength;
     }
-    if (ck.s2_on && (ctl & kCtlS2)) ist = (R)gd.s2_strength;
+    if (ck.s2_on && (ctl & kCtlS2)) ist = gd.s2_strength;
 
     CellState<R> c;
     load_cell(c, gd.s, k);
     c.v = vc;
-    StepOut o{0.0};
+    StepOut<R> o{};
     tpord_step<R>(c, ctl & kCtlType, gd.model, kst, ist, du, &o);
     store_cell(c, gd.s, k);
     Vn[g] = c.v;
@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(256) k_grid_step(GridDev<R> gd, StepK kst, int
             const uint8_t ph0 = ds.phase;
             const float vp0 = ds.vpeak;
             const uint8_t e0 = ds.ead;
-            if (det_step(ds, (float)vc, (float)c.v, (float)o.dvdt, (float)ck.time, gd.act_thr, t_act, ev)) {
+            if (det_step(ds, (float)vc, (float)c.v, (float)o.dvdt, ck.time_f, gd.act_thr, t_act, ev)) {
                 if (ev.t_90 >= 0.f) gd.apd90[k] = ev.apd90;
             }
             dirty |= ds.phase != ph0 || ds.vpeak != vp0 || ds.ead != e0;
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(256) k_grid_step(GridDev<R> gd, StepK kst, int
         }
     }
     const R vn = c.v;
-    const bool bad = !(vn == vn) || vn < (R)gd.vmin_ok || vn > (R)gd.vmax_ok;
+    const bool bad = !(vn == vn) || vn < gd.vmin_ok || vn > gd.vmax_ok;
     const unsigned m = __ballot_sync(__activemask(), bad);
     if (m && (threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(gd.nbad, (unsigned long long)__popc(m));
 }
@@ -150,6 +150,7 @@ __global__ void __launch_bounds__(256) k_ghost(GridDev<R> gd, int nxt)
         Clock ck = *gd.clk;
         ck.step += 1;
         ck.time += gd.dt;
+        ck.time_f = (float)ck.time;
         int32_t w = ck.widx;
         while (w < gd.nwin && ck.step >= gd.win[w].off) ++w;
         ck.widx = w;

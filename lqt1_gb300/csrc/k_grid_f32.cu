@@ -8,9 +8,10 @@ cudaError_t launch_grid_step<float>(const GridDev<float> &gd, const StepK &k, in
 {
     if (gd.ntissue <= 0) return cudaSuccess;
     const unsigned nb = (unsigned)((gd.ntissue + 255) / 256);
-    if (dim == 1) k_grid_step<float, 1><<<nb, 256, 0, st>>>(gd, k, cur);
-    else if (dim == 2) k_grid_step<float, 2><<<nb, 256, 0, st>>>(gd, k, cur);
-    else k_grid_step<float, 3><<<nb, 256, 0, st>>>(gd, k, cur);
+    const StepT<float> kk = step_as<float>(k);
+    if (dim == 1) k_grid_step<float, 1><<<nb, 256, 0, st>>>(gd, kk, cur);
+    else if (dim == 2) k_grid_step<float, 2><<<nb, 256, 0, st>>>(gd, kk, cur);
+    else k_grid_step<float, 3><<<nb, 256, 0, st>>>(gd, kk, cur);
     return cudaGetLastError();
 }
 

@@ -8,9 +8,10 @@ cudaError_t launch_grid_step<double>(const GridDev<double> &gd, const StepK &k, 
 {
     if (gd.ntissue <= 0) return cudaSuccess;
     const unsigned nb = (unsigned)((gd.ntissue + 255) / 256);
-    if (dim == 1) k_grid_step<double, 1><<<nb, 256, 0, st>>>(gd, k, cur);
-    else if (dim == 2) k_grid_step<double, 2><<<nb, 256, 0, st>>>(gd, k, cur);
-    else k_grid_step<double, 3><<<nb, 256, 0, st>>>(gd, k, cur);
+    const StepT<double> kk = step_as<double>(k);
+    if (dim == 1) k_grid_step<double, 1><<<nb, 256, 0, st>>>(gd, kk, cur);
+    else if (dim == 2) k_grid_step<double, 2><<<nb, 256, 0, st>>>(gd, kk, cur);
+    else k_grid_step<double, 3><<<nb, 256, 0, st>>>(gd, kk, cur);
     return cudaGetLastError();
 }
 

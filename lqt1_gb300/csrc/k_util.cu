@@ -13,8 +13,17 @@ __global__ void k_pack(const double *__restrict__ aos, SoA<R> s, int64_t n)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const double *a = aos + i * 40;
-        s.v[i] = (R)a[0];
-        for (int j = 0; j < kNConc; ++j) s.conc[j * s.ld + i] = a[1 + j];
+        if (s.v) s.v[i] = (R)a[0];
+        if (sizeof(R) == 8) {
+            for (int j = 0; j < kNConc; ++j) s.conc[j * s.ld + i] = a[1 + j];
+        } else {
+            float *f = reinterpret_cast<float *>(s.conc);
+            for (int j = 0; j < kNConc; ++j) {
+                const float hi = (float)a[1 + j];
+                f[j * s.ld + i] = hi;
+                f[(8 + j) * s.ld + i] = (float)(a[1 + j] - (double)hi);
+            }
+        }
         for (int j = 0; j < kNGate; ++j) s.gate[j * s.ld + i] = (R)a[9 + j];
     }
 }
@@ -24,8 +33,13 @@ __global__ void k_unpack(SoA<R> s, double *__restrict__ aos, int64_t n)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         double *a = aos + i * 40;
-        a[0] = (double)s.v[i];
-        for (int j = 0; j < kNConc; ++j) a[1 + j] = s.conc[j * s.ld + i];
+        a[0] = s.v ? (double)s.v[i] : 0.0;
+        if (sizeof(R) == 8) {
+            for (int j = 0; j < kNConc; ++j) a[1 + j] = s.conc[j * s.ld + i];
+        } else {
+            const float *f = reinterpret_cast<const float *>(s.conc);
+            for (int j = 0; j < kNConc; ++j) a[1 + j] = (double)f[j * s.ld + i] + (double)f[(8 + j) * s.ld + i];
+        }
         for (int j = 0; j < kNGate; ++j) a[9 + j] = (double)s.gate[j * s.ld + i];
     }
 }

@@ -59,6 +59,7 @@ template <typename R> struct BatchDev {
     int32_t max_beats;
     const Win *win;
     const ModelK *models;
+    double dt;                       // for the FP64 time accumulation (OneD.cc:317)
     int *queue;                      // atomic work counter
     unsigned long long *nbad;        // blow-up counter
     double vmin_ok, vmax_ok;

@@ -9,10 +9,13 @@
 //                the host (same glibc values the reference computes).
 //   R = float  : the mixed form.  Gates, currents and fluxes in FP32 with the
 //                hardware exp2/log2/rcp approximations; the eight
-//                concentrations stay FP64 and every difference of two
-//                concentrations (Jdiff*, Jtr) is taken in FP64 before rounding,
-//                because at rest kss - ki is ~1e-5 mM against an FP32 ulp of
-//                1.5e-5 mM at 145 mM.  GHK terms use x/expm1(x), finite at V = 0.
+//                concentrations are Kahan-compensated FP32 pairs (hi + lo,
+//                about 48 significant bits, the same 8 bytes as FP64) and every
+//                difference of two concentrations (Jdiff*, Jtr) is formed from
+//                both parts, because at rest kss - ki is ~1e-5 mM against an
+//                FP32 ulp of 1.5e-5 mM at 145 mM.  No FP64 instruction is left
+//                on this path: GB300 issues FP64 at about 1/64 of the FP32 rate.
+//                GHK terms use x/expm1(x), finite at V = 0.
 //
 // States hsp and jp are carried in the state vector but never change (their
 // ORd INa is commented out in SingleCell/TPORd.cc:436-460), so the step does
@@ -24,23 +27,63 @@
 
 namespace lqt {
 
-// Scenario parameters as the kernels use them (from lqt_model, include/lqt.h).
-// PCa and GKs per cell class (0 endo, 1 epi, 2 mid) are computed on the host
-// in the reference's order (TPORd.cc:622-639 and 692-733: base value, ISO1,
-// type factor; LQT1, SUPREP, ISO1), so the FP64 form sees the same doubles.
-struct ModelK {
-    double pca[3];
-    double gks[3];
-    double dss_shift, fss_shift;     // ISO1 gate shifts (TPORd.cc:582,588)
+// Scenario parameters (from lqt_model, include/lqt.h).  PCa and GKs per cell
+// class (0 endo, 1 epi, 2 mid) are computed on the host in the reference's
+// order (TPORd.cc:622-639 and 692-733: base value, ISO1, type factor; LQT1,
+// SUPREP, ISO1), so the FP64 form sees the same doubles.
+template <typename R> struct ModelT {
+    R pca[3];
+    R gks[3];
+    R dss_shift, fss_shift;          // ISO1 gate shifts (TPORd.cc:582,588)
 };
+using ModelK = ModelT<double>;
 
-__device__ __forceinline__ int cell_class(int ctype) { return ctype == 2 ? 1 : (ctype == 4 ? 2 : 0); }
+template <typename R> __host__ __device__ inline ModelT<R> model_as(const ModelK &m)
+{
+    ModelT<R> o;
+    for (int i = 0; i < 3; ++i) {
+        o.pca[i] = (R)m.pca[i];
+        o.gks[i] = (R)m.gks[i];
+    }
+    o.dss_shift = m.dss_shift;
+    o.fss_shift = m.fss_shift;
+    return o;
+}
 
 // Per-step constants computed on the host with glibc, shared by all cells.
-struct StepK {
-    double dt;
-    double e_hl, e_hlp, e_jca;       // exp(-dt/200), exp(-dt/600), exp(-dt/75) (TPORd.cc:517-521,605-606)
+template <typename R> struct StepT {
+    R dt;
+    R e_hl, e_hlp, e_jca;            // exp(-dt/200), exp(-dt/600), exp(-dt/75) (TPORd.cc:517-521,605-606)
 };
+using StepK = StepT<double>;
+
+template <typename R> __host__ __device__ inline StepT<R> step_as(const StepK &k)
+{
+    return StepT<R>{(R)k.dt, (R)k.e_hl, (R)k.e_hlp, (R)k.e_jca};
+}
+
+// ---- concentration storage -------------------------------------------------
+// FP64 form: double.  Mixed form: float2 {hi, lo} with hi + lo the value.
+template <typename R> struct ConcOf { using T = double; };
+template <> struct ConcOf<float> { using T = float2; };
+
+__device__ __forceinline__ double cval(double c) { return c; }
+__device__ __forceinline__ float cval(float2 c) { return c.x; }
+__device__ __forceinline__ double cdiff(double a, double b) { return a - b; }
+__device__ __forceinline__ float cdiff(float2 a, float2 b) { return __fadd_rn(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y)); }
+__device__ __forceinline__ void cadd(double &c, double inc) { c += inc; }
+// c += inc as a compensated sum (TwoSum of hi and inc, error folded into lo,
+// renormalised); the _rn intrinsics keep the compiler from contracting it.
+__device__ __forceinline__ void cadd(float2 &c, float inc)
+{
+    const float s = __fadd_rn(c.x, inc);
+    const float bb = __fsub_rn(s, c.x);
+    const float e = __fadd_rn(__fsub_rn(c.x, __fsub_rn(s, bb)), __fsub_rn(inc, bb));
+    const float l = __fadd_rn(c.y, e);
+    const float h = __fadd_rn(s, l);
+    c.y = __fsub_rn(l, __fsub_rn(h, s));
+    c.x = h;
+}
 
 // ---- math policy ----------------------------------------------------------
 template <typename R> struct Mth;
@@ -74,27 +117,28 @@ __device__ __forceinline__ float x_over_expm1(float x, float em1)
 
 // ---- cell state in registers ---------------------------------------------
 template <typename R> struct CellState {
+    using C = typename ConcOf<R>::T;
     R v;
-    double nai, nass, ki, kss, cai, cass, cansr, cajsr;
+    C nai, nass, ki, kss, cai, cass, cansr, cajsr;
     R sm, sh, sj, mL, hL, hLp, a, iF, iS, ap, iFp, iSp, d, ff, fs;
     R fcaf, fcas, jca, nca, ffp, fcafp, xrf, xrs, xs1, xs2, xk1;
     R Jrelnp, Jrelp, CaMKt;
 };
 
-struct StepOut {
-    double dvdt;   // -(Iion + Ist) (TPORd.cc:928)
+template <typename R> struct StepOut {
+    R dvdt;        // -(Iion + Ist) (TPORd.cc:928)
 };
 
 // One TPORd update.  ctype: 2 = EPI, 4 = MCELL, other = endocardial
 // (SingleCell/Cell.cc:20; only EPI and MCELL change parameters).
 template <typename R>
-__device__ __forceinline__ void tpord_step(CellState<R> &c, int ctype, const ModelK &m, const StepK &k,
-                                           R Ist, R dVgap_dt, StepOut *out)
+__device__ __forceinline__ void tpord_step(CellState<R> &c, int ctype, const ModelT<R> &m, const StepT<R> &k,
+                                           R Ist, R dVgap_dt, StepOut<R> *out)
 {
     using M = Mth<R>;
     const bool epi = (ctype == 2);
     const bool mid = (ctype == 4);
-    const R dt = (R)k.dt;
+    const R dt = k.dt;
     const R v = c.v;
 
     // constants, TPORd.cc:382-421
@@ -110,8 +154,8 @@ __device__ __forceinline__ void tpord_step(CellState<R> &c, int ctype, const Mod
     constexpr double FFRT = F_ * F_ / (R_ * T_);
     constexpr double FRT = F_ / (R_ * T_);
 
-    const R nai = (R)c.nai, nass = (R)c.nass, ki = (R)c.ki, kss = (R)c.kss;
-    const R cai = (R)c.cai, cass = (R)c.cass, cajsr = (R)c.cajsr, cansr = (R)c.cansr;
+    const R nai = cval(c.nai), nass = cval(c.nass), ki = cval(c.ki), kss = cval(c.kss);
+    const R cai = cval(c.cai), cass = cval(c.cass), cajsr = cval(c.cajsr), cansr = cval(c.cansr);
 
     // reversal potentials, TPORd.cc:425-427
     const R ENa = (R)RTF * M::lg(M::dv((R)nao, nai));
@@ -166,9 +210,9 @@ __device__ __forceinline__ void tpord_step(CellState<R> &c, int ctype, const Mod
                                  (R)8.552 * M::ex(M::dk(-(v + (R)77.42), 5.955)));
     c.mL = mLss - (mLss - c.mL) * M::ex(M::dv(-dt, tm));
     const R hLss = M::dv((R)1, (R)1 + M::ex(M::dk(v + (R)87.61, 7.488)));
-    c.hL = hLss - (hLss - c.hL) * (R)k.e_hl;
+    c.hL = hLss - (hLss - c.hL) * k.e_hl;
     const R hLssp = M::dv((R)1, (R)1 + M::ex(M::dk(v + (R)93.81, 7.488)));
-    c.hLp = hLssp - (hLssp - c.hLp) * (R)k.e_hlp;
+    c.hLp = hLssp - (hLssp - c.hLp) * k.e_hlp;
     const R GNaL = epi ? (R)(0.0075 * 0.6) : (R)0.0075;
     const R INaL = GNaL * (v - ENa) * c.mL * (((R)1 - fP) * c.hL + fP * c.hLp);
 
@@ -205,10 +249,10 @@ __device__ __forceinline__ void tpord_step(CellState<R> &c, int ctype, const Mod
     const R Ito = Gto * (v - EK) * (((R)1 - fP) * c.a * ii + fP * c.ap * ip);
 
     // ICaL, ICaNa, ICaK, TPORd.cc:573-652
-    const R dss = M::dv((R)1, (R)1 + M::ex(M::dk(-(v + (R)3.940 + (R)m.dss_shift), 4.230)));
+    const R dss = M::dv((R)1, (R)1 + M::ex(M::dk(-(v + (R)3.940 + m.dss_shift), 4.230)));
     const R td = (R)0.6 + M::dv((R)1, M::ex((R)-0.05 * (v + (R)6)) + M::ex((R)0.09 * (v + (R)14)));
     c.d = dss - (dss - c.d) * M::ex(M::dv(-dt, td));
-    const R fss = M::dv((R)1, (R)1 + M::ex(M::dk(v + (R)19.58 + (R)m.fss_shift, 3.696)));
+    const R fss = M::dv((R)1, (R)1 + M::ex(M::dk(v + (R)19.58 + m.fss_shift, 3.696)));
     const R tff = (R)7 + M::dv((R)1, (R)0.0045 * M::ex(M::dk(-(v + (R)20), 10.)) +
                                      (R)0.0045 * M::ex(M::dk(v + (R)20, 10.)));
     const R tfs = (R)1000 + M::dv((R)1, (R)0.000035 * M::ex(M::dk(-(v + (R)5), 4.)) +
@@ -226,7 +270,7 @@ __device__ __forceinline__ void tpord_step(CellState<R> &c, int ctype, const Mod
     c.fcaf = fcass - (fcass - c.fcaf) * M::ex(M::dv(-dt, tfcaf));
     c.fcas = fcass - (fcass - c.fcas) * M::ex(M::dv(-dt, tfcas));
     const R fca = Afcaf * c.fcaf + Afcas * c.fcas;
-    c.jca = fcass - (fcass - c.jca) * (R)k.e_jca;
+    c.jca = fcass - (fcass - c.jca) * k.e_jca;
     c.ffp = fss - (fss - c.ffp) * M::ex(M::dv(-dt, (R)2.5 * tff));
     const R fp = (R)Aff * c.ffp + (R)Afs * c.fs;
     c.fcafp = fcass - (fcass - c.fcafp) * M::ex(M::dv(-dt, (R)2.5 * tfcaf));
@@ -262,7 +306,7 @@ __device__ __forceinline__ void tpord_step(CellState<R> &c, int ctype, const Mod
         ICab_phi = 4.0f * g2 * (cai * e2 - (float)(0.341 * cao));
     }
     const int cls = epi ? 1 : (mid ? 2 : 0);
-    const R PCa = (R)m.pca[cls];
+    const R PCa = m.pca[cls];
     const R PCap = (R)1.1 * PCa;
     const R gate_np = c.d * (f * ((R)1 - c.nca) + c.jca * fca * c.nca);
     const R gate_p = c.d * (fp * ((R)1 - c.nca) + c.jca * fcap * c.nca);
@@ -296,7 +340,7 @@ __device__ __forceinline__ void tpord_step(CellState<R> &c, int ctype, const Mod
     else
         c.xs2 = xs1ss - (xs1ss - c.xs2) * M::ex(-dt * rate_xs2);
     const R KsCa = (R)1 + M::dv((R)0.6, (R)1 + M::pw(M::dv((R)3.8e-5, cai), (R)1.4));
-    const R IKs = (R)m.gks[cls] * KsCa * c.xs1 * c.xs2 * (v - EKs);
+    const R IKs = m.gks[cls] * KsCa * c.xs1 * c.xs2 * (v - EKs);
 
     // IK1, TPORd.cc:738-751 (sqrt(ko) constant)
     const R xk1ss = M::dv((R)1, (R)1 + M::ex(M::dk(-(v + (R)(2.5538 * ko + 144.59)), 1.5692 * ko + 3.8115)));
@@ -402,15 +446,15 @@ __device__ __forceinline__ void tpord_step(CellState<R> &c, int ctype, const Mod
     const R Iion = INa + INaL + Ito + ICaL + ICaNa + ICaK + IKr + IKs + IK1 + INaCa + INaK + INab + IKb + IpCa + ICab;
     const R dV_dt = (R)-1 * (Iion + Ist);
     c.v = v + (dV_dt + dVgap_dt) * dt;
-    if (out) out->dvdt = (double)dV_dt;
+    if (out) out->dvdt = dV_dt;
 
     // CaMK and fluxes, TPORd.cc:939-995
     c.CaMKt += dt * ((R)0.05 * CaMKb * (CaMKb + c.CaMKt) - (R)0.00068 * c.CaMKt);
-    // concentration differences in FP64 (see file comment)
-    const R JdiffNa = (R)((c.nass - c.nai) * 0.5);
-    const R JdiffK = (R)((c.kss - c.ki) * 0.5);
-    const R Jdiff = (R)((c.cass - c.cai) / 0.2);
-    const R Jtr = (R)((c.cansr - c.cajsr) / 100.0);
+    // concentration differences from the full-precision values (file comment)
+    const R JdiffNa = cdiff(c.nass, c.nai) * (R)0.5;
+    const R JdiffK = cdiff(c.kss, c.ki) * (R)0.5;
+    const R Jdiff = M::dk(cdiff(c.cass, c.cai), 0.2);
+    const R Jtr = M::dk(cdiff(c.cansr, c.cajsr), 100.);
     {
         const R r15 = M::dv((R)1.5, cajsr);
         const R r2 = r15 * r15, r4 = r2 * r2;
@@ -439,7 +483,7 @@ __device__ __forceinline__ void tpord_step(CellState<R> &c, int ctype, const Mod
     const R Jleak = M::dk((R)0.0039375 * cansr, 15.);
     const R Jup = ((R)1 - fP) * Jupnp + fP * Jupp - Jleak;
 
-    // concentrations, forward Euler in FP64 storage, TPORd.cc:997-1020
+    // concentrations, forward Euler, TPORd.cc:997-1020
     const R dnai = -(INa + INaL + (R)3 * INaCa_i + (R)3 * INaK + INab) * (R)(Acap / (F_ * vmyo)) + JdiffNa * (R)(vss / vmyo);
     const R dnass = -(ICaNa + (R)3 * INaCa_ss) * (R)(Acap / (F_ * vss)) - JdiffNa;
     const R dki = -(Ito + IKr + IKs + IK1 + IKb + Ist - (R)2 * INaK) * (R)(Acap / (F_ * vmyo)) + JdiffK * (R)(vss / vmyo);
@@ -459,15 +503,14 @@ __device__ __forceinline__ void tpord_step(CellState<R> &c, int ctype, const Mod
     const R qj = (R)kmcsqn + cajsr;
     const R Bcajsr = M::dv((R)1, (R)1 + M::dv((R)(csqnmax * kmcsqn), qj * qj));
     const R dcajsr = Bcajsr * (Jtr - Jrel);
-    const double dtd = k.dt;
-    c.nai += dtd * (double)dnai;
-    c.nass += dtd * (double)dnass;
-    c.ki += dtd * (double)dki;
-    c.kss += dtd * (double)dkss;
-    c.cai += dtd * (double)dcai;
-    c.cass += dtd * (double)dcass;
-    c.cansr += dtd * (double)dcansr;
-    c.cajsr += dtd * (double)dcajsr;
+    cadd(c.nai, dt * dnai);
+    cadd(c.nass, dt * dnass);
+    cadd(c.ki, dt * dki);
+    cadd(c.kss, dt * dkss);
+    cadd(c.cai, dt * dcai);
+    cadd(c.cass, dt * dcass);
+    cadd(c.cansr, dt * dcansr);
+    cadd(c.cajsr, dt * dcajsr);
 }
 
 }  // namespace lqt

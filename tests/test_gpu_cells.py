@@ -64,7 +64,7 @@ def test_mixed_one_step_close_to_oracle(lq, orc):
     got = c.get_state()
     assert np.abs(got[:, 0] - ref[:, 0]).max() < 2e-3           # mV
     assert np.abs(got[:, 9:37] - ref[:, 9:37]).max() < 1e-4     # gates
-    np.testing.assert_allclose(got[:, 1:9], ref[:, 1:9], rtol=1e-6)
+    np.testing.assert_allclose(got[:, 1:9], ref[:, 1:9], rtol=1e-5)
 
 
 def test_state_roundtrip_and_dump(lq, orc, tmp_path):
