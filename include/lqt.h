@@ -294,6 +294,24 @@ int lqt_sim_profile(lqt_sim *s, int64_t nsteps, double *ms_step, double *ms_ghos
 int lqt_sim_boundary(const lqt_sim *s, int64_t *dst_host, int64_t *src_host,
                      int64_t *n);
 
+/* Pseudo-ECG of a caller-owned V grid that allocates nothing (no counterpart
+ * in the reference).  For callers that cannot call cudaMalloc: a host framework
+ * that owns all device memory and hands out fixed buffers, or a stepping loop
+ * that must not take the device-wide synchronisation of cudaMalloc/cudaFree.
+ * Same sum as lqt_sim_set_electrodes / lqt_sim_get_ecg.  v_grid_dev: FP32 V of
+ * the nx*ny*nz grid with mirror ghosts filled (1D: the strand itself);
+ * tissue_index_dev: int32 grid index of each tissue voxel (NULL for 1D);
+ * electrodes_host: nel*3 mm; phi_dev: nel doubles written on `stream`.
+ * Limits: 1 <= nel <= 8; ntissue and the grid below 2^31.  Its scratch is a
+ * fixed 128 KiB device array inside the library (every GPU that loads the
+ * library holds it until exit); the first call on a device looks up that
+ * array's address, so make it before any stream capture.  Calls that overlap
+ * on the GPU share the array and race: serialise them. */
+int lqt_ecg_grid_noalloc(const float *v_grid_dev, int32_t nx, int32_t ny,
+                         int32_t nz, double dx, const int32_t *tissue_index_dev,
+                         int64_t ntissue, const double *electrodes_host,
+                         int32_t nel, double *phi_dev, void *stream);
+
 /* Blow-up detector: count of voxels with NaN or V outside [vmin_ok, vmax_ok]
  * since the last call (GPU3D.cu:1796-1829 does this scan on the host). */
 int lqt_sim_check(lqt_sim *s, int64_t *n_bad);
