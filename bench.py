@@ -233,6 +233,7 @@ def main():
     sim.set_electrodes(np.array(w["electrodes"]), every=50)
     n = sim.n
     sim.step(args.prerun)
+    variant, tune_ms = sim.tune(-1)          # occupancy variant of the step kernel
     sim.step(args.warmup)
     torch.cuda.synchronize()
 
@@ -323,7 +324,9 @@ def main():
             "config": {"workload": w["desc"], "tissue_voxels": n, "form": "mixed (FP32 gates/currents/diffusion, "
                        "FP64 concentrations)", "dt_ms": 0.02, "electrodes": len(w["electrodes"]),
                        "l2": "inputs larger than L2 (state %.2f GB/step)" % (BYTES_MIXED * n / 1e9),
-                       "parallelism": f"replicas x{world}"},
+                       "parallelism": f"replicas x{world}",
+                       "step_kernel_variant": {"min_ctas_per_sm": variant,
+                                               "tuned_ms": [round(float(x), 4) for x in tune_ms[:3]]}},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "fp64_form": fp64,
             "gpu_launches": 2 * args.steps + ecg_launches, "clocks": clocks, "blowup_voxel_steps": nbad}
     print(json.dumps(line), flush=True)

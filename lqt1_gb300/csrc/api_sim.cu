@@ -67,6 +67,10 @@ struct lqt_sim {
     float4 *el = nullptr;
     double *ecg_partial = nullptr, *ecg_out = nullptr, *ecg_t = nullptr;
     int64_t *ecg_count = nullptr, ecg_cap = 0;
+    // occupancy variant of k_grid_step (minimum CTAs/SM) and the autotuner
+    int minb = 2;
+    bool tuned = false;
+    float tune_ms[4] = {0, 0, 0, 0};
     // graph
     cudaGraphExec_t graph = nullptr;
     int graph_cur = -1;
@@ -200,11 +204,11 @@ int launch_step(lqt_sim *s)
     const StepK k = make_stepk(s->p.dt);
     if (s->fp64()) {
         const GridDev<double> g = devf<double>(s);
-        CK(launch_grid_step<double>(g, k, s->cur, s->dim, s->stream));
+        CK(launch_grid_step<double>(g, k, s->cur, s->dim, s->minb, s->stream));
         CK(launch_ghost<double>(g, s->cur ^ 1, s->stream));
     } else {
         const GridDev<float> g = devf<float>(s);
-        CK(launch_grid_step<float>(g, k, s->cur, s->dim, s->stream));
+        CK(launch_grid_step<float>(g, k, s->cur, s->dim, s->minb, s->stream));
         CK(launch_ghost<float>(g, s->cur ^ 1, s->stream));
     }
     s->cur ^= 1;
@@ -231,6 +235,63 @@ int step_once(lqt_sim *s)
     s->time += s->p.dt;
     if (s->nel > 0 && s->ecg_every > 0 && s->step % s->ecg_every == 0) return launch_ecg_now(s);
     return LQT_OK;
+}
+
+// Autotuner: time `per` real steps with each occupancy variant of the step
+// kernel (CUDA events around the step kernel only) and keep the fastest.  The
+// variants differ only in register allocation, so the steps are valid
+// simulation steps whichever variant runs them.  Returns the steps consumed.
+int autotune(lqt_sim *s, int per, int64_t *consumed)
+{
+    const int *cand = s->fp64() ? kGridVariantsF64 : kGridVariantsF32;
+    const int ncand = s->dim == 1 ? 1 : (s->fp64() ? 2 : 3);
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    float best = 1e30f;
+    int best_m = cand[0];
+    int rc = LQT_OK;
+    *consumed = 0;
+    for (int c = 0; c < ncand && rc == LQT_OK; ++c) {
+        s->minb = cand[c];
+        float tot = 0.f;
+        for (int i = 0; i < per && rc == LQT_OK; ++i) {
+            cudaError_t e = cudaEventRecord(a, s->stream);
+            const StepK k = make_stepk(s->p.dt);
+            if (e == cudaSuccess)
+                e = s->fp64() ? launch_grid_step<double>(devf<double>(s), k, s->cur, s->dim, s->minb, s->stream)
+                              : launch_grid_step<float>(devf<float>(s), k, s->cur, s->dim, s->minb, s->stream);
+            if (e == cudaSuccess) e = cudaEventRecord(b, s->stream);
+            if (e == cudaSuccess)
+                e = s->fp64() ? launch_ghost<double>(devf<double>(s), s->cur ^ 1, s->stream)
+                              : launch_ghost<float>(devf<float>(s), s->cur ^ 1, s->stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(b);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+            if (e != cudaSuccess) {
+                rc = fail(LQT_ERR_CUDA, std::string("autotune: ") + cudaGetErrorString(e));
+                break;
+            }
+            s->cur ^= 1;
+            s->step += 1;
+            s->time += s->p.dt;
+            ++*consumed;
+            if (s->nel > 0 && s->ecg_every > 0 && s->step % s->ecg_every == 0) rc = launch_ecg_now(s);
+            if (i > 0) tot += ms;     // the first launch of a variant pays its module load
+        }
+        const float avg = per > 1 ? tot / (per - 1) : tot;
+        if (c < 4) s->tune_ms[c] = avg;
+        if (avg < best) {
+            best = avg;
+            best_m = cand[c];
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    s->minb = best_m;
+    s->tuned = true;
+    s->graph_valid = false;
+    return rc;
 }
 
 int build_graph(lqt_sim *s)
@@ -319,6 +380,7 @@ int lqt_sim_create(const lqt_sim_params *params, const lqt_geometry *geom, lqt_s
     }
     auto *s = new lqt_sim();
     s->p = p;
+    s->minb = p.precision == LQT_FP64 ? 1 : 2;
     s->nx = nx;
     s->ny = ny;
     s->nz = nz;
@@ -521,6 +583,12 @@ int lqt_sim_step(lqt_sim *s, int64_t nsteps)
         if (rc) return rc;
     }
     int64_t left = nsteps;
+    if (!s->tuned && left >= 64) {
+        int64_t used = 0;
+        int rc = autotune(s, 5, &used);
+        if (rc) return rc;
+        left -= used;
+    }
     while (left > 0) {
         // graph replay for whole chunks starting on a chunk boundary
         if (left >= kGraphChunk && s->step % kGraphChunk == 0 &&
@@ -696,6 +764,29 @@ int lqt_sim_get_detect(lqt_sim *s, float *t_act, float *apd90, uint8_t *ead)
     return LQT_OK;
 }
 
+int lqt_sim_tune(lqt_sim *s, int32_t variant, int32_t *chosen, float *ms_per_variant)
+{
+    if (!s) return fail(LQT_ERR_INVALID, "lqt_sim_tune: NULL handle");
+    if (variant >= 0) {
+        const int *cand = s->fp64() ? kGridVariantsF64 : kGridVariantsF32;
+        const int ncand = s->fp64() ? 2 : 3;
+        bool ok = false;
+        for (int c = 0; c < ncand; ++c) ok |= cand[c] == variant;
+        if (!ok) return fail(LQT_ERR_INVALID, "lqt_sim_tune: variant must be 2, 3 or 4 (mixed) or 1, 2 (FP64)");
+        s->minb = variant;
+        s->tuned = true;
+        s->graph_valid = false;
+    } else {
+        int64_t used = 0;
+        int rc = autotune(s, 5, &used);
+        if (rc) return rc;
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    if (chosen) *chosen = s->minb;
+    if (ms_per_variant) std::memcpy(ms_per_variant, s->tune_ms, sizeof(s->tune_ms));
+    return LQT_OK;
+}
+
 int lqt_sim_profile(lqt_sim *s, int64_t nsteps, double *ms_step, double *ms_ghost)
 {
     if (!s || nsteps <= 0) return fail(LQT_ERR_INVALID, "lqt_sim_profile: NULL handle or nsteps <= 0");
@@ -708,12 +799,12 @@ int lqt_sim_profile(lqt_sim *s, int64_t nsteps, double *ms_step, double *ms_ghos
         cudaError_t e = cudaEventRecord(ev[0], s->stream);
         if (s->fp64()) {
             const GridDev<double> g = devf<double>(s);
-            if (e == cudaSuccess) e = launch_grid_step<double>(g, k, s->cur, s->dim, s->stream);
+            if (e == cudaSuccess) e = launch_grid_step<double>(g, k, s->cur, s->dim, s->minb, s->stream);
             if (e == cudaSuccess) e = cudaEventRecord(ev[1], s->stream);
             if (e == cudaSuccess) e = launch_ghost<double>(g, s->cur ^ 1, s->stream);
         } else {
             const GridDev<float> g = devf<float>(s);
-            if (e == cudaSuccess) e = launch_grid_step<float>(g, k, s->cur, s->dim, s->stream);
+            if (e == cudaSuccess) e = launch_grid_step<float>(g, k, s->cur, s->dim, s->minb, s->stream);
             if (e == cudaSuccess) e = cudaEventRecord(ev[1], s->stream);
             if (e == cudaSuccess) e = launch_ghost<float>(g, s->cur ^ 1, s->stream);
         }

@@ -54,8 +54,14 @@ template <typename R> struct GridDev {
     unsigned long long *nbad;
 };
 
+// Occupancy variants of k_grid_step: minimum CTAs/SM of 256 threads.
+constexpr int kGridVariantsF32[3] = {2, 3, 4};
+constexpr int kGridVariantsF64[2] = {1, 2};
+
 template <typename R>
-cudaError_t launch_grid_step(const GridDev<R> &gd, const StepK &k, int cur, int dim, cudaStream_t st);
+cudaError_t launch_grid_step(const GridDev<R> &gd, const StepK &k, int cur, int dim, int minb, cudaStream_t st);
+template <typename R>
+cudaError_t launch_grid_step_minb(const GridDev<R> &gd, const StepT<R> &k, int cur, int dim, int minb, cudaStream_t st);
 template <typename R> cudaError_t launch_ghost(const GridDev<R> &gd, int nxt, cudaStream_t st);
 template <typename R>
 cudaError_t launch_ecg(const GridDev<R> &gd, int cur, const float4 *el, int nel, double *partial, double *out,

@@ -71,8 +71,11 @@ __device__ __forceinline__ R grid_du(const GridDev<R> &gd, const R *__restrict__
     }
 }
 
-template <typename R, int DIM>
-__global__ void __launch_bounds__(256) k_grid_step(GridDev<R> gd, StepT<R> kst, int cur)
+// MINB = minimum resident CTAs per SM the register allocation must allow
+// (occupancy variants picked at run time by the autotuner in api_sim.cu; they
+// differ only in register allocation, not in arithmetic).
+template <typename R, int DIM, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_grid_step(GridDev<R> gd, StepT<R> kst, int cur)
 {
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k >= gd.ntissue) return;

@@ -1,18 +1,17 @@
-// k_grid_f32.cu -- instantiations of the grid kernels (k_grid.cuh) for R = float.
+// k_grid_f32.cu -- grid kernels for the mixed form (R = float): launchers, the
+// default occupancy variant and the pseudo-ECG.
 #include "k_grid.cuh"
 
 namespace lqt {
 
-template <>
-cudaError_t launch_grid_step<float>(const GridDev<float> &gd, const StepK &k, int cur, int dim, cudaStream_t st)
+template <> cudaError_t launch_grid_step_minb<float>(const GridDev<float> &gd, const StepT<float> &kk, int cur,
+                                                     int dim, int minb, cudaStream_t st);
+
+template <> cudaError_t launch_grid_step<float>(const GridDev<float> &gd, const StepK &k, int cur, int dim, int minb,
+                                                cudaStream_t st)
 {
     if (gd.ntissue <= 0) return cudaSuccess;
-    const unsigned nb = (unsigned)((gd.ntissue + 255) / 256);
-    const StepT<float> kk = step_as<float>(k);
-    if (dim == 1) k_grid_step<float, 1><<<nb, 256, 0, st>>>(gd, kk, cur);
-    else if (dim == 2) k_grid_step<float, 2><<<nb, 256, 0, st>>>(gd, kk, cur);
-    else k_grid_step<float, 3><<<nb, 256, 0, st>>>(gd, kk, cur);
-    return cudaGetLastError();
+    return launch_grid_step_minb<float>(gd, step_as<float>(k), cur, dim, minb, st);
 }
 
 template <> cudaError_t launch_ghost<float>(const GridDev<float> &gd, int nxt, cudaStream_t st)
@@ -26,7 +25,7 @@ template <> cudaError_t launch_ghost<float>(const GridDev<float> &gd, int nxt, c
 
 template <>
 cudaError_t launch_ecg<float>(const GridDev<float> &gd, int cur, const float4 *el, int nel, double *partial, double *out,
-                           double *t_out, int64_t *counter, int64_t cap, int dim, cudaStream_t st)
+                              double *t_out, int64_t *counter, int64_t cap, int dim, cudaStream_t st)
 {
     const int64_t nb = ecg_blocks(gd.ntissue);
     if (dim == 1) k_ecg_partial<float, 1><<<(unsigned)nb, 256, 0, st>>>(gd, gd.vg[cur], el, nel, partial);
@@ -35,10 +34,6 @@ cudaError_t launch_ecg<float>(const GridDev<float> &gd, int cur, const float4 *e
     k_ecg_final<<<1, 256, 0, st>>>(partial, nb, nel, out, t_out, counter, cap, gd.clk);
     return cudaGetLastError();
 }
-
-}  // namespace lqt
-
-namespace lqt {
 
 int64_t ecg_blocks(int64_t ntissue) { return ntissue <= 0 ? 1 : (ntissue + 255) / 256; }
 

@@ -1,0 +1,16 @@
+// k_grid_f32_d3.cu -- occupancy variants of the 3D mixed-form step kernel
+// (separate translation unit so the variants compile in parallel).
+#include "k_grid.cuh"
+
+namespace lqt {
+
+cudaError_t launch_f32_d3(const GridDev<float> &gd, const StepT<float> &kk, int cur, int minb, cudaStream_t st)
+{
+    const unsigned nb = (unsigned)((gd.ntissue + 255) / 256);
+    if (minb >= 4) k_grid_step<float, 3, 4><<<nb, 256, 0, st>>>(gd, kk, cur);
+    else if (minb == 3) k_grid_step<float, 3, 3><<<nb, 256, 0, st>>>(gd, kk, cur);
+    else k_grid_step<float, 3, 2><<<nb, 256, 0, st>>>(gd, kk, cur);
+    return cudaGetLastError();
+}
+
+}  // namespace lqt

@@ -101,6 +101,16 @@ class Sim:
         s = np.ascontiguousarray(s, dtype=np.float64)
         N.check(N.lib().lqt_sim_set_state(self._h, _p(s)), "lqt_sim_set_state")
 
+    def tune(self, variant: int = -1):
+        """Force an occupancy variant of the step kernel (>= 0) or autotune now (-1).
+        Returns (chosen variant, ms per candidate)."""
+        L = N.lib()
+        L.lqt_sim_tune.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.c_void_p]
+        ch = C.c_int32()
+        ms = np.zeros(4, np.float32)
+        N.check(L.lqt_sim_tune(self._h, int(variant), C.byref(ch), _p(ms)), "lqt_sim_tune")
+        return ch.value, ms
+
     def profile(self, nsteps: int = 20):
         """Mean device ms per launch of the fused step kernel and of the ghost
         kernel (CUDA events on the simulation's stream)."""
