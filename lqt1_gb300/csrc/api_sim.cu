@@ -451,6 +451,16 @@ int lqt_sim_create(const lqt_sim_params *params, const lqt_geometry *geom, lqt_s
         return fail(LQT_ERR_NOMEM, "lqt_sim_create: " + m);
     }
     cudaStream_t st = s->stream;
+    // the device clock is read by k_ghost, which set_state below launches:
+    // give it a defined value before any kernel runs
+    {
+        Clock c0{};
+        c0.s1_cycle_ok = 1;
+        if (cudaMemcpy(s->clk, &c0, sizeof(c0), cudaMemcpyHostToDevice) != cudaSuccess) {
+            delete s;
+            return fail(LQT_ERR_CUDA, "lqt_sim_create: clock upload failed");
+        }
+    }
     // per-voxel control bytes and maps
     s->ctl_host.resize(n);
     for (int64_t k = 0; k < n; ++k) s->ctl_host[k] = geom->cell_type[s->tm.cells[k]] & kCtlType;

@@ -154,11 +154,12 @@ __global__ void __launch_bounds__(256) k_ghost(GridDev<R> gd, int nxt)
         ck.step += 1;
         ck.time += gd.dt;
         ck.time_f = (float)ck.time;
-        int32_t w = ck.widx;
-        while (w < gd.nwin && ck.step >= gd.win[w].off) ++w;
+        int32_t w = ck.widx < 0 ? 0 : ck.widx;
+        const int32_t nwin = gd.win ? gd.nwin : 0;
+        while (w < nwin && ck.step >= gd.win[w].off) ++w;
         ck.widx = w;
-        ck.s1_on = w < gd.nwin && ck.step >= gd.win[w].on;
-        ck.opened = w < gd.nwin && ck.step == gd.win[w].on;
+        ck.s1_on = w < nwin && ck.step >= gd.win[w].on;
+        ck.opened = w < nwin && ck.step == gd.win[w].on;
         ck.s2_on = ck.step >= gd.s2_win.on && ck.step < gd.s2_win.off;
         if (gd.onset) {
             ck.tb = ck.time - floor(ck.time / gd.bcl) * gd.bcl;
