@@ -192,6 +192,8 @@ def main():
     ap.add_argument("--prerun", type=int, default=1000, help="untimed steps to start the wave (setup)")
     ap.add_argument("--fp64-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sweep-beats", type=int, default=2,
+                    help="beats of the 4096-instance batched sweep leg (0 = skip; 20 = the full sweep)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -308,6 +310,20 @@ def main():
                 "achieved_gbs": BYTES_FP64 * n / (ms64 / 1e3) / 1e9, "mixed_over_fp64": value / (v64 * world)}
         s64.close()
 
+    # batched sweep leg: 4096 uneven single cells / strands (50-400 cells), own
+    # parameters each, one persistent graph-captured launch (autotuned shape)
+    sweep = None
+    if args.sweep_beats > 0:
+        insts, models, _ = lq.batch.sweep(n=4096, seed=2024, beats=args.sweep_beats)
+        bt = lq.Batch(insts, models, precision=lq.MIXED, max_beats=args.sweep_beats + 1,
+                      stream=stream.cuda_stream)
+        work = sum(len(x.types) * round(x.t_stop / 0.02) for x in insts)
+        ms_sw = bt.run()
+        sweep = {"value": world * work / (ms_sw / 1e3), "unit": UNIT, "instances": len(insts), "cells": bt.ncells,
+                 "beats": args.sweep_beats, "device_ms": ms_sw, "launch": bt.config(),
+                 "blowup_cell_steps": bt.num_bad(), "form": "mixed"}
+        bt.close()
+
     if rank != 0:
         return
     cpu = None
@@ -327,7 +343,7 @@ def main():
                        "parallelism": f"replicas x{world}",
                        "step_kernel_variant": {"min_ctas_per_sm": variant,
                                                "tuned_ms": [round(float(x), 4) for x in tune_ms[:3]]}},
-            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "fp64_form": fp64,
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "fp64_form": fp64, "batched_sweep": sweep,
             "gpu_launches": 2 * args.steps + ecg_launches, "clocks": clocks, "blowup_voxel_steps": nbad}
     print(json.dumps(line), flush=True)
 

@@ -164,9 +164,11 @@ typedef struct lqt_batch_params {
     int32_t precision;         /* LQT_FP64 or LQT_MIXED */
     int32_t max_beats;         /* detector slots per cell */
     int64_t rec_every;         /* steps between V records (10 in OneD.cc:402) */
-    int32_t threads;           /* CTA width; 0 = autotuned */
-    int32_t ctas;              /* persistent CTAs; 0 = autotuned */
-    void *stream;              /* cudaStream_t or NULL */
+    int32_t threads;           /* CTA width 128/256/512; 0 = autotuned */
+    int32_t ctas;              /* persistent CTAs; 0 = resident CTAs x SMs */
+    void *stream;              /* cudaStream_t, or NULL for an owned stream (the
+                                  run is a CUDA graph, which cannot be captured
+                                  on the legacy default stream) */
 } lqt_batch_params;
 
 /* cell_types: all cells, instance by instance (sum of ncells).
@@ -189,6 +191,11 @@ int lqt_batch_get_record(lqt_batch *b, int32_t inst, float *v, double *t,
                          double *ecg, int64_t cap, int64_t *nrec);
 int lqt_batch_get_state(lqt_batch *b, double *state_host);
 int lqt_batch_set_state(lqt_batch *b, const double *state_host);
+/* The launch configuration the autotuner chose (threads = 0 in the params):
+ * CTA width, minimum resident CTAs/SM of the kernel variant, persistent CTAs
+ * and the number of work items. */
+int lqt_batch_config(const lqt_batch *b, int32_t *threads, int32_t *minb,
+                     int32_t *ctas, int32_t *nitems);
 /* Device time of the last run, ms (CUDA events on the batch stream). */
 double lqt_batch_last_run_ms(const lqt_batch *b);
 /* Blow-up counter of the last run (voxel-steps with NaN or V out of range). */

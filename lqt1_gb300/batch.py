@@ -77,6 +77,14 @@ class Batch:
         N.check(N.lib().lqt_batch_run(self._h), "lqt_batch_run")
         return float(N.lib().lqt_batch_last_run_ms(self._h))
 
+    def config(self):
+        """Launch configuration chosen by the autotuner."""
+        L = N.lib()
+        L.lqt_batch_config.argtypes = [C.c_void_p] + [C.POINTER(C.c_int32)] * 4
+        v = [C.c_int32() for _ in range(4)]
+        N.check(L.lqt_batch_config(self._h, *[C.byref(x) for x in v]), "lqt_batch_config")
+        return dict(threads=v[0].value, min_ctas_per_sm=v[1].value, ctas=v[2].value, nitems=v[3].value)
+
     def num_bad(self) -> int:
         return int(N.lib().lqt_batch_num_bad(self._h))
 
@@ -150,3 +158,37 @@ class OneDStrand:
             out["cv_start"] = s[0] if s else float("nan")
             out["cv_end"] = e[0] if e else float("nan")
         return out
+
+
+def sweep(n=4096, seed=2024, beats=20, p_single=0.5, len_range=(50, 400), bcl_range=(400.0, 2000.0),
+          stim_duration=2.0, stim_strength=-52.0, record=0):
+    """Seeded sweep of uneven instances (the batched-sweep workload).
+
+    Each instance is a single cell (probability p_single, random type) or a
+    strand of U{len_range} cells (OneD.cc's 25/35/40 % endo/M/epi split), with
+    its own model: IKs mutation fraction f ~ U[0,1] giving GKs x (1 - 0.95 f)
+    (f = 1 is the reference's LQT1 factor 0.05, TPORd.cc:706), beta-adrenergic
+    ICaL and IKs multipliers ~ U[1,2] (PCa and GKs ISO factors), BCL ~ U(bcl_range),
+    `beats` stimulated cycles; stimulus 2 ms x -52 pA/pF at 50 ms.
+    Returns (instances, models, params) with params per instance."""
+    rng = np.random.default_rng(seed)
+    insts, models, params = [], [], []
+    for i in range(n):
+        single = rng.random() < p_single
+        if single:
+            types = np.array([rng.choice([N.ENDO, N.MCELL, N.EPI])], np.uint8)
+        else:
+            L = int(rng.integers(len_range[0], len_range[1] + 1))
+            ne, nm = int(round(0.25 * L)), int(round(0.35 * L))
+            types = np.array([N.ENDO] * ne + [N.MCELL] * nm + [N.EPI] * (L - ne - nm), np.uint8)
+        f = float(rng.random())
+        ical = float(rng.uniform(1.0, 2.0))
+        iks = float(rng.uniform(1.0, 2.0))
+        bcl = float(rng.uniform(*bcl_range))
+        m = N.model("baseline", gks_scale=1.0 - 0.95 * f, pca_scale=ical, gks_iso_scale=iks)
+        models.append(m)
+        insts.append(InstanceSpec(types=types, model=i, bcl=bcl, s1_start=50.0, s1_duration=stim_duration,
+                                  s1_strength=stim_strength, s1_beats=beats, n_stim=1 if single else 3, dx=0.15,
+                                  t_stop=beats * bcl, record=i < record))
+        params.append(dict(single=single, mut=f, ical=ical, iks=iks, bcl=bcl, ncells=len(types)))
+    return insts, models, params

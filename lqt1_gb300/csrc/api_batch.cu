@@ -23,6 +23,12 @@ struct lqt_batch {
     float last_ms = 0.f;
     DevMem mem;
     std::vector<int64_t> perm;          // internal cell -> input cell
+    std::vector<int> order;             // internal order of instances
+    int max_strand = 1;
+    int minb = 1;
+    bool own_stream = false;
+    std::vector<std::pair<std::pair<int, int>, float>> tuned;   // ((width, minb), probe ms)
+    cudaGraphExec_t graph = nullptr;
     std::vector<lqt_instance> inst;
     std::vector<int64_t> inst_cell0;    // input order: first cell of each instance
     std::vector<int64_t> inst_internal0;// internal first cell of each instance
@@ -51,8 +57,10 @@ struct lqt_batch {
 
     ~lqt_batch()
     {
+        if (graph) cudaGraphExecDestroy(graph);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        if (own_stream && stream) cudaStreamDestroy(stream);
     }
     template <typename R> BatchDev<R> dev() const
     {
@@ -69,6 +77,7 @@ struct lqt_batch {
         b.win = win;
         b.models = models;
         b.dt = p.dt;
+        b.step_cap = 0;
         b.queue = queue;
         b.nbad = nbad;
         b.vmin_ok = -200.0;
@@ -93,6 +102,142 @@ static int upload(void *dst, const void *src, size_t bytes, cudaStream_t st)
     if (bytes == 0) return LQT_OK;
     CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
     return LQT_OK;
+}
+
+// Next-fit partition of the internal order into items of at most W cells;
+// a recorded strand gets an item of its own (its pseudo-ECG is per item).
+static std::vector<Item> make_items(const lqt_batch *b, int W)
+{
+    std::vector<Item> items;
+    Item cur{};
+    auto flush = [&]() {
+        if (cur.ncells > 0) items.push_back(cur);
+        cur = Item{};
+    };
+    for (int oi : b->order) {
+        const lqt_instance &q = b->inst[oi];
+        const bool own = q.record && q.ncells > 1;
+        if (own || cur.ncells + q.ncells > W) flush();
+        if (cur.ncells == 0) {
+            cur.cell0 = b->inst_internal0[oi];
+            cur.nsteps = 0;
+            cur.ecg_seg = -1;
+        }
+        cur.ncells += q.ncells;
+        cur.nsteps = std::max(cur.nsteps, b->inst_nsteps[oi]);
+        if (own) {
+            cur.ecg_seg = oi;
+            flush();
+        }
+    }
+    flush();
+    return items;
+}
+
+static int set_items(lqt_batch *b, int W, int minb)
+{
+    std::vector<Item> items = make_items(b, W);
+    CK(cudaMemcpyAsync(b->items, items.data(), items.size() * sizeof(Item), cudaMemcpyHostToDevice, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    b->nitems = (int32_t)items.size();
+    b->threads = W;
+    b->minb = minb;
+    int dev = 0, nsm = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int per_sm = b->p.precision == LQT_FP64 ? batch_max_ctas_per_sm<double>(W, minb)
+                                                  : batch_max_ctas_per_sm<float>(W, minb);
+    b->ctas = b->p.ctas > 0 ? b->p.ctas : std::max(1, std::min(b->nitems, nsm * std::max(1, per_sm)));
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    return LQT_OK;
+}
+
+static int launch_run(lqt_batch *b, int64_t step_cap)
+{
+    cudaStream_t st = b->stream;
+    CK(cudaMemsetAsync(b->queue, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(b->nbad, 0, sizeof(unsigned long long), st));
+    if (b->p.max_beats > 0) {
+        const int64_t nb = b->ncells * b->p.max_beats;
+        CK(cudaMemsetAsync(b->det_t_act, 0xff, nb * 4, st));   // 0xffffffff = NaN -> reported as -1
+        CK(cudaMemsetAsync(b->det_apd90, 0xff, nb * 4, st));
+        CK(cudaMemsetAsync(b->det_dvdt, 0xff, nb * 4, st));
+        CK(cudaMemsetAsync(b->det_ead, 0, b->ncells, st));
+        CK(cudaMemsetAsync(b->det_beats, 0, b->ncells * 4, st));
+    }
+    if (b->p.precision == LQT_FP64) {
+        BatchDev<double> d = b->dev<double>();
+        d.step_cap = step_cap;
+        CK(launch_batch<double>(d, make_stepk(b->p.dt), b->threads, b->minb, b->ctas, st));
+    } else {
+        BatchDev<float> d = b->dev<float>();
+        d.step_cap = step_cap;
+        CK(launch_batch<float>(d, make_stepk(b->p.dt), b->threads, b->minb, b->ctas, st));
+    }
+    return LQT_OK;
+}
+
+// Autotuner: every (CTA width, min CTAs/SM) variant that fits the longest
+// strand runs a capped probe (the same cells x steps for all) from a snapshot
+// of the state, which is restored afterwards; the fastest is kept.
+static int tune_batch(lqt_batch *b)
+{
+    auto all = b->p.precision == LQT_FP64 ? batch_variants<double>() : batch_variants<float>();
+    std::vector<std::pair<int, int>> cand;
+    for (auto &v : all)
+        if (v.first >= b->max_strand && (b->p.threads == 0 || v.first == b->p.threads)) cand.push_back(v);
+    if (cand.empty()) return fail(LQT_ERR_INVALID, "no kernel variant fits the longest strand");
+    if (cand.size() == 1) return set_items(b, cand[0].first, cand[0].second);
+    const size_t rsz = b->p.precision == LQT_FP64 ? 8 : 4;
+    const size_t bytes_v = b->ld * rsz, bytes_g = b->ld * rsz * kNGate, bytes_c = b->ld * 8 * kNConc;
+    void *snap = nullptr;
+    CK(cudaMalloc(&snap, bytes_v + bytes_g + bytes_c));
+    char *sp = (char *)snap;
+    cudaStream_t st = b->stream;
+    int rc = LQT_OK;
+    auto copy_all = [&](bool save) -> int {
+        CK(cudaMemcpyAsync(save ? sp : b->v, save ? b->v : sp, bytes_v, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(save ? sp + bytes_v : b->gate, save ? b->gate : sp + bytes_v, bytes_g,
+                           cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(save ? sp + bytes_v + bytes_g : (char *)b->conc, save ? (char *)b->conc : sp + bytes_v + bytes_g,
+                           bytes_c, cudaMemcpyDeviceToDevice, st));
+        return LQT_OK;
+    };
+    int64_t max_ns = 0;
+    for (auto ns : b->inst_nsteps) max_ns = std::max(max_ns, ns);
+    const int64_t cap = std::min<int64_t>(max_ns, 400);
+    rc = copy_all(true);
+    float best = 1e30f;
+    std::pair<int, int> pick = cand[0];
+    b->tuned.clear();
+    for (size_t c = 0; c < cand.size() && !rc; ++c) {
+        rc = set_items(b, cand[c].first, cand[c].second);
+        if (rc) break;
+        rc = launch_run(b, 8);                 // warm the variant's module
+        if (!rc) rc = copy_all(false);
+        if (!rc) {
+            cudaError_t e = cudaEventRecord(b->ev0, st);
+            if (e == cudaSuccess) rc = launch_run(b, cap);
+            if (!rc && e == cudaSuccess) e = cudaEventRecord(b->ev1, st);
+            if (e == cudaSuccess) e = cudaEventSynchronize(b->ev1);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+            if (e != cudaSuccess && !rc) rc = fail(LQT_ERR_CUDA, std::string("batch autotune: ") + cudaGetErrorString(e));
+            b->tuned.push_back({cand[c], ms});
+            if (!rc && ms < best) {
+                best = ms;
+                pick = cand[c];
+            }
+        }
+        if (!rc) rc = copy_all(false);
+    }
+    if (!rc) rc = set_items(b, pick.first, pick.second);
+    cudaStreamSynchronize(st);
+    cudaFree(snap);
+    return rc;
 }
 
 extern "C" {
@@ -137,13 +282,20 @@ int lqt_batch_create(const lqt_batch_params *params, int32_t ninst, const lqt_in
     b->ncells = ncells;
     b->ld = pad128(ncells);
     b->stream = (cudaStream_t)p.stream;
-    b->inst.assign(inst, inst + ninst);
-    b->threads = p.threads > 0 ? p.threads : (max_strand <= 128 ? 128 : (max_strand <= 256 ? 256 : 512));
-    if (b->threads != 128 && b->threads != 256 && b->threads != 512) {
-        delete b;
-        return fail(LQT_ERR_INVALID, "lqt_batch_create: threads must be 128, 256 or 512");
+    if (!b->stream) {
+        // the run is captured as a CUDA graph: not on the legacy default stream
+        if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete b;
+            return fail(LQT_ERR_CUDA, "lqt_batch_create: cannot create a stream");
+        }
+        b->own_stream = true;
     }
-    if (max_strand > b->threads) {
+    b->inst.assign(inst, inst + ninst);
+    if (p.threads != 0 && p.threads != 128 && p.threads != 256 && p.threads != 512) {
+        delete b;
+        return fail(LQT_ERR_INVALID, "lqt_batch_create: threads must be 0 (autotune), 128, 256 or 512");
+    }
+    if (p.threads > 0 && max_strand > p.threads) {
         delete b;
         return fail(LQT_ERR_INVALID, "lqt_batch_create: a strand is longer than the CTA width");
     }
@@ -160,7 +312,10 @@ int lqt_batch_create(const lqt_batch_params *params, int32_t ninst, const lqt_in
         stim_windows(times, ns, p.dt, q.bcl, q.s1_start, q.s1_duration, q.s1_beats, wins[i]);
     }
 
-    // items: strands alone, single cells packed by step count; largest first
+    // Fixed internal order: recorded strands first (each gets its own item,
+    // for its pseudo-ECG), then every instance by step count, longest first.
+    // Items for a CTA width W are a next-fit partition of this order, so the
+    // state layout does not depend on W and the autotuner can try widths.
     b->inst_cell0.resize(ninst);
     for (int i = 0, c0 = 0; i < ninst; ++i) {
         b->inst_cell0[i] = c0;
@@ -169,12 +324,12 @@ int lqt_batch_create(const lqt_batch_params *params, int32_t ninst, const lqt_in
     std::vector<int> order(ninst);
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
-        const int64_t wa = b->inst_nsteps[a] * ((inst[a].ncells + 31) / 32);
-        const int64_t wc = b->inst_nsteps[c] * ((inst[c].ncells + 31) / 32);
-        if (inst[a].ncells > 1 || inst[c].ncells > 1) return wa > wc;
-        return b->inst_nsteps[a] > b->inst_nsteps[c];
+        const bool ra = inst[a].record && inst[a].ncells > 1, rc2 = inst[c].record && inst[c].ncells > 1;
+        if (ra != rc2) return ra;
+        if (b->inst_nsteps[a] != b->inst_nsteps[c]) return b->inst_nsteps[a] > b->inst_nsteps[c];
+        return inst[a].ncells > inst[c].ncells;
     });
-    std::vector<Item> items;
+    b->order = order;
     std::vector<Seg> segs(ninst);
     std::vector<Win> allwin;
     b->inst_internal0.assign(ninst, 0);
@@ -182,60 +337,40 @@ int lqt_batch_create(const lqt_batch_params *params, int32_t ninst, const lqt_in
     b->rec_slot.assign(ninst, -1);
     int32_t nrec_slots = 0;
     int64_t next_cell = 0;
-    Item cur{};
-    cur.ncells = 0;
-    auto flush = [&]() {
-        if (cur.ncells > 0) items.push_back(cur);
-        cur = Item{};
-        cur.ncells = 0;
-    };
     for (int oi : order) {
         const lqt_instance &q = inst[oi];
-        const bool single = q.ncells == 1;
-        if (!single || cur.ncells + 1 > b->threads) flush();
-        if (cur.ncells == 0) {
-            cur.cell0 = next_cell;
-            cur.nsteps = 0;
-            cur.ecg_seg = -1;
-        }
-        Seg s{};
-        s.cell0 = next_cell;
-        s.nsteps = b->inst_nsteps[oi];
-        s.n = q.ncells;
-        s.n_stim = q.n_stim;
-        s.model = q.model;
-        s.win0 = (int32_t)allwin.size();
-        s.nwin = (int32_t)wins[oi].size();
+        Seg sg{};
+        sg.cell0 = next_cell;
+        sg.nsteps = b->inst_nsteps[oi];
+        sg.n = q.ncells;
+        sg.n_stim = q.n_stim;
+        sg.model = q.model;
+        sg.win0 = (int32_t)allwin.size();
+        sg.nwin = (int32_t)wins[oi].size();
         allwin.insert(allwin.end(), wins[oi].begin(), wins[oi].end());
-        s.dx = q.dx;
-        s.stim = q.s1_strength;
-        s.ecg_x0 = q.ecg_x0;
-        s.act_thr = (float)q.act_threshold;
-        s.rec_slot = -1;
+        sg.dx = q.dx;
+        sg.stim = q.s1_strength;
+        sg.ecg_x0 = q.ecg_x0;
+        sg.act_thr = (float)q.act_threshold;
+        sg.rec_slot = -1;
         if (q.record) {
-            s.rec_slot = nrec_slots++;
-            b->rec_slot[oi] = s.rec_slot;
+            sg.rec_slot = nrec_slots++;
+            b->rec_slot[oi] = sg.rec_slot;
             b->rec_width = std::max(b->rec_width, (int32_t)q.ncells);
-            if (!single) cur.ecg_seg = oi;
         }
-        segs[oi] = s;
+        segs[oi] = sg;
         b->inst_internal0[oi] = next_cell;
         for (int j = 0; j < q.ncells; ++j) b->perm[next_cell + j] = b->inst_cell0[oi] + j;
         next_cell += q.ncells;
-        cur.ncells += q.ncells;
-        cur.nsteps = std::max(cur.nsteps, s.nsteps);
-        if (!single) flush();
     }
-    flush();
-    b->nitems = (int32_t)items.size();
+    b->max_strand = max_strand;
     // segments are indexed by input instance; cell -> segment map (internal order)
     std::vector<int32_t> seg_of(ncells);
     for (int i = 0; i < ninst; ++i)
         for (int j = 0; j < inst[i].ncells; ++j) seg_of[b->inst_internal0[i] + j] = i;
-    int64_t max_ns = 0;
-    for (auto ns : b->inst_nsteps) max_ns = std::max(max_ns, ns);
-    b->rec_cap = nrec_slots ? (max_ns + p.rec_every - 1) / p.rec_every : 0;
-
+    int64_t max_ns_all = 0;
+    for (auto ns : b->inst_nsteps) max_ns_all = std::max(max_ns_all, ns);
+    b->rec_cap = nrec_slots ? (max_ns_all + p.rec_every - 1) / p.rec_every : 0;
     // per-cell inputs in internal order; dD/dx per strand as OneD.cc:123-131
     std::vector<uint8_t> ct(ncells);
     std::vector<double> co(ncells), dco(ncells);
@@ -273,7 +408,7 @@ int lqt_batch_create(const lqt_batch_params *params, int32_t ninst, const lqt_in
     rc |= b->mem.alloc((void **)&b->dcoeff, ncells * 8);
     rc |= b->mem.alloc((void **)&b->seg_of, ncells * 4);
     rc |= b->mem.alloc((void **)&b->segs, ninst * sizeof(Seg));
-    rc |= b->mem.alloc((void **)&b->items, items.size() * sizeof(Item));
+    rc |= b->mem.alloc((void **)&b->items, ninst * sizeof(Item));
     rc |= b->mem.alloc((void **)&b->win, allwin.size() * sizeof(Win));
     rc |= b->mem.alloc((void **)&b->models, nmodels * sizeof(ModelK));
     rc |= b->mem.alloc((void **)&b->queue, 16);
@@ -301,7 +436,6 @@ int lqt_batch_create(const lqt_batch_params *params, int32_t ninst, const lqt_in
     rc = upload(b->ctype, ct.data(), ncells, st) | upload(b->coeff, co.data(), ncells * 8, st) |
          upload(b->dcoeff, dco.data(), ncells * 8, st) | upload(b->seg_of, seg_of.data(), ncells * 4, st) |
          upload(b->segs, segs.data(), ninst * sizeof(Seg), st) |
-         upload(b->items, items.data(), items.size() * sizeof(Item), st) |
          upload(b->win, allwin.data(), allwin.size() * sizeof(Win), st) |
          upload(b->models, mk.data(), nmodels * sizeof(ModelK), st) |
          upload(b->aos, init_int.data(), ncells * 320, st);
@@ -320,12 +454,12 @@ int lqt_batch_create(const lqt_batch_params *params, int32_t ninst, const lqt_in
         delete b;
         return fail(LQT_ERR_CUDA, std::string("lqt_batch_create: ") + cudaGetErrorString(e));
     }
-    int dev = 0, nsm = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int per_sm = p.precision == LQT_FP64 ? batch_max_ctas_per_sm<double>(b->threads)
-                                               : batch_max_ctas_per_sm<float>(b->threads);
-    b->ctas = p.ctas > 0 ? p.ctas : std::max(1, std::min(b->nitems, nsm * std::max(1, per_sm)));
+    rc = tune_batch(b);
+    if (rc) {
+        std::string m = g_err;
+        delete b;
+        return fail(rc, "lqt_batch_create: " + m);
+    }
     *out = b;
     return LQT_OK;
 }
@@ -338,22 +472,36 @@ int lqt_batch_run(lqt_batch *b)
 {
     if (!b) return fail(LQT_ERR_INVALID, "lqt_batch_run: NULL handle");
     cudaStream_t st = b->stream;
-    CK(cudaMemsetAsync(b->queue, 0, sizeof(int), st));
-    CK(cudaMemsetAsync(b->nbad, 0, sizeof(unsigned long long), st));
-    if (b->p.max_beats > 0) {
-        const int64_t nb = b->ncells * b->p.max_beats;
-        CK(cudaMemsetAsync(b->det_t_act, 0xff, nb * 4, st));   // 0xffffffff = NaN -> reported as -1
-        CK(cudaMemsetAsync(b->det_apd90, 0xff, nb * 4, st));
-        CK(cudaMemsetAsync(b->det_dvdt, 0xff, nb * 4, st));
-        CK(cudaMemsetAsync(b->det_ead, 0, b->ncells, st));
-        CK(cudaMemsetAsync(b->det_beats, 0, b->ncells * 4, st));
+    if (!b->graph) {
+        // the whole run (resets + one persistent launch) as one CUDA graph
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        int rc = launch_run(b, 0);
+        cudaError_t e = cudaStreamEndCapture(st, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return fail(LQT_ERR_CUDA, std::string("lqt_batch_run capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(LQT_ERR_CUDA, std::string("lqt_batch_run instantiate: ") + cudaGetErrorString(e));
     }
     CK(cudaEventRecord(b->ev0, st));
-    CK(b->p.precision == LQT_FP64 ? launch_batch<double>(b->dev<double>(), make_stepk(b->p.dt), b->threads, b->ctas, st)
-                                  : launch_batch<float>(b->dev<float>(), make_stepk(b->p.dt), b->threads, b->ctas, st));
+    CK(cudaGraphLaunch(b->graph, st));
     CK(cudaEventRecord(b->ev1, st));
     CK(cudaEventSynchronize(b->ev1));
     CK(cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1));
+    return LQT_OK;
+}
+
+int lqt_batch_config(const lqt_batch *b, int32_t *threads, int32_t *minb, int32_t *ctas, int32_t *nitems)
+{
+    if (!b) return fail(LQT_ERR_INVALID, "lqt_batch_config: NULL handle");
+    if (threads) *threads = b->threads;
+    if (minb) *minb = b->minb;
+    if (ctas) *ctas = b->ctas;
+    if (nitems) *nitems = b->nitems;
     return LQT_OK;
 }
 

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/lqt.h"
@@ -52,6 +53,7 @@ void stim_windows(const std::vector<double> &times, int64_t nsteps, double dt, d
                   int beats, std::vector<Win> &out);
 int64_t pad128(int64_t n);
 
-template <typename R> int batch_max_ctas_per_sm(int threads);
+template <typename R> int batch_max_ctas_per_sm(int threads, int minb);
+template <typename R> std::vector<std::pair<int, int>> batch_variants();
 
 }  // namespace lqt

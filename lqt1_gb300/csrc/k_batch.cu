@@ -48,9 +48,11 @@ __global__ void __launch_bounds__(128) k_cells_update(SoA<R> s, const uint8_t *_
 }
 
 // ------------------------------------------------------------------------
-// Persistent batch kernel.
-template <typename R, int MAXT>
-__global__ void __launch_bounds__(MAXT) k_batch(BatchDev<R> b, StepT<R> k)
+// Persistent batch kernel.  MAXT = CTA width (cells per item), MINB = minimum
+// resident CTAs per SM the register allocation must allow (the autotuner in
+// api_batch.cu picks the pair).
+template <typename R, int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) k_batch(BatchDev<R> b, StepT<R> k)
 {
     __shared__ R vbuf[2][MAXT];
     __shared__ double red[MAXT / 32];
@@ -105,7 +107,9 @@ __global__ void __launch_bounds__(MAXT) k_batch(BatchDev<R> b, StepT<R> k)
         int cur = 0;
         vbuf[0][t] = active ? c.v : (R)0;
 
-        for (int64_t st = 0; st < item.nsteps; ++st) {
+        const int64_t nsteps_item = b.step_cap > 0 && b.step_cap < item.nsteps ? b.step_cap : item.nsteps;
+        const int64_t nsteps_seg = b.step_cap > 0 && b.step_cap < seg.nsteps ? b.step_cap : seg.nsteps;
+        for (int64_t st = 0; st < nsteps_item; ++st) {
             __syncthreads();
             // pseudo-ECG of the previous recorded step (needs all V of that step)
             if (item.ecg_seg >= 0 && st > 0 && ((st - 1) % b.rec_every) == 0) {
@@ -129,7 +133,7 @@ __global__ void __launch_bounds__(MAXT) k_batch(BatchDev<R> b, StepT<R> k)
                     if (slot < b.rec_cap) b.ecg[(int64_t)b.segs[item.ecg_seg].rec_slot * b.rec_cap + slot] = acc;
                 }
             }
-            if (active && st < seg.nsteps) {
+            if (active && st < nsteps_seg) {
                 const R *V = vbuf[cur];
                 const R vo = V[t];
                 // diffusion, OneD.cc:366-391 (mirrored ends)
@@ -201,7 +205,7 @@ __global__ void __launch_bounds__(MAXT) k_batch(BatchDev<R> b, StepT<R> k)
         }
         // ECG of the final recorded step
         __syncthreads();
-        if (item.ecg_seg >= 0 && item.nsteps > 0 && ((item.nsteps - 1) % b.rec_every) == 0) {
+        if (item.ecg_seg >= 0 && nsteps_item > 0 && ((nsteps_item - 1) % b.rec_every) == 0) {
             double term = 0.0;
             if (active) {
                 const R *V = vbuf[cur];
@@ -218,7 +222,7 @@ __global__ void __launch_bounds__(MAXT) k_batch(BatchDev<R> b, StepT<R> k)
             if (t == 0) {
                 double acc = 0.0;
                 for (int w = 0; w < (int)(blockDim.x >> 5); ++w) acc += red[w];
-                const int64_t slot = (item.nsteps - 1) / b.rec_every;
+                const int64_t slot = (nsteps_item - 1) / b.rec_every;
                 if (slot < b.rec_cap) b.ecg[(int64_t)b.segs[item.ecg_seg].rec_slot * b.rec_cap + slot] = acc;
             }
         }
@@ -245,17 +249,27 @@ cudaError_t launch_cells_update(const SoA<R> &s, const uint8_t *ctype, const dou
     return cudaGetLastError();
 }
 
+// (width, minimum CTAs/SM) variants compiled for each precision
+#define LQT_BATCH_VARIANTS_F32(X) X(float, 128, 4) X(float, 128, 6) X(float, 256, 2) X(float, 256, 3) X(float, 512, 1)
+#define LQT_BATCH_VARIANTS_F64(X) X(double, 128, 1) X(double, 256, 1) X(double, 512, 1)
+
 template <typename R>
-cudaError_t launch_batch(const BatchDev<R> &b, const StepK &k, int threads, int ctas, cudaStream_t stream)
+cudaError_t launch_batch(const BatchDev<R> &b, const StepK &k, int threads, int minb, int ctas, cudaStream_t stream)
 {
     if (b.nitems <= 0) return cudaSuccess;
-    if (threads <= 128)
-        k_batch<R, 128><<<ctas, 128, 0, stream>>>(b, step_as<R>(k));
-    else if (threads <= 256)
-        k_batch<R, 256><<<ctas, 256, 0, stream>>>(b, step_as<R>(k));
-    else
-        k_batch<R, 512><<<ctas, 512, 0, stream>>>(b, step_as<R>(k));
-    return cudaGetLastError();
+    const StepT<R> kk = step_as<R>(k);
+#define LQT_LAUNCH(RR, T, M)                                                                   \
+    if (sizeof(R) == sizeof(RR) && threads == T && minb == M) {                                \
+        k_batch<R, T, M><<<ctas, T, 0, stream>>>(b, kk);                                       \
+        return cudaGetLastError();                                                             \
+    }
+    if constexpr (sizeof(R) == 4) {
+        LQT_BATCH_VARIANTS_F32(LQT_LAUNCH)
+    } else {
+        LQT_BATCH_VARIANTS_F64(LQT_LAUNCH)
+    }
+#undef LQT_LAUNCH
+    return cudaErrorInvalidConfiguration;
 }
 
 template cudaError_t launch_cells_update<double>(const SoA<double> &, const uint8_t *, const double *,
@@ -264,25 +278,43 @@ template cudaError_t launch_cells_update<double>(const SoA<double> &, const uint
 template cudaError_t launch_cells_update<float>(const SoA<float> &, const uint8_t *, const double *, const double *,
                                                 double *, const ModelK *, const uint16_t *, const StepK &, int64_t,
                                                 int64_t, cudaStream_t);
-template cudaError_t launch_batch<double>(const BatchDev<double> &, const StepK &, int, int, cudaStream_t);
-template cudaError_t launch_batch<float>(const BatchDev<float> &, const StepK &, int, int, cudaStream_t);
+template cudaError_t launch_batch<double>(const BatchDev<double> &, const StepK &, int, int, int, cudaStream_t);
+template cudaError_t launch_batch<float>(const BatchDev<float> &, const StepK &, int, int, int, cudaStream_t);
 
 }  // namespace lqt
 
 namespace lqt {
-// Resident CTAs per SM for the batch kernel at a given width (autotuner input).
-template <typename R> int batch_max_ctas_per_sm(int threads)
+// Resident CTAs per SM of a variant, and the variant list (autotuner input).
+template <typename R> int batch_max_ctas_per_sm(int threads, int minb)
 {
     int n = 0;
-    cudaError_t e;
-    if (threads <= 128)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch<R, 128>, 128, 0);
-    else if (threads <= 256)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch<R, 256>, 256, 0);
-    else
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch<R, 512>, 512, 0);
-    return e == cudaSuccess ? n : 1;
+    cudaError_t e = cudaErrorInvalidConfiguration;
+#define LQT_OCC(RR, T, M)                                                                      \
+    if (sizeof(R) == sizeof(RR) && threads == T && minb == M)                                  \
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch<R, T, M>, T, 0);
+    if constexpr (sizeof(R) == 4) {
+        LQT_BATCH_VARIANTS_F32(LQT_OCC)
+    } else {
+        LQT_BATCH_VARIANTS_F64(LQT_OCC)
+    }
+#undef LQT_OCC
+    return e == cudaSuccess ? n : 0;
 }
-template int batch_max_ctas_per_sm<double>(int);
-template int batch_max_ctas_per_sm<float>(int);
+template int batch_max_ctas_per_sm<double>(int, int);
+template int batch_max_ctas_per_sm<float>(int, int);
+
+template <typename R> std::vector<std::pair<int, int>> batch_variants()
+{
+    std::vector<std::pair<int, int>> v;
+#define LQT_LIST(RR, T, M) v.emplace_back(T, M);
+    if constexpr (sizeof(R) == 4) {
+        LQT_BATCH_VARIANTS_F32(LQT_LIST)
+    } else {
+        LQT_BATCH_VARIANTS_F64(LQT_LIST)
+    }
+#undef LQT_LIST
+    return v;
+}
+template std::vector<std::pair<int, int>> batch_variants<double>();
+template std::vector<std::pair<int, int>> batch_variants<float>();
 }  // namespace lqt

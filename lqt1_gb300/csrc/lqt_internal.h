@@ -60,6 +60,7 @@ template <typename R> struct BatchDev {
     const Win *win;
     const ModelK *models;
     double dt;                       // for the FP64 time accumulation (OneD.cc:317)
+    int64_t step_cap;                // > 0: stop every item after this many steps (autotuner probes)
     int *queue;                      // atomic work counter
     unsigned long long *nbad;        // blow-up counter
     double vmin_ok, vmax_ok;
@@ -80,7 +81,7 @@ cudaError_t launch_cells_update(const SoA<R> &s, const uint8_t *ctype, const dou
                                 double *dvdt, const ModelK *models, const uint16_t *model_of, const StepK &k,
                                 int64_t n, int64_t nsteps, cudaStream_t stream);
 template <typename R>
-cudaError_t launch_batch(const BatchDev<R> &b, const StepK &k, int threads, int ctas, cudaStream_t stream);
+cudaError_t launch_batch(const BatchDev<R> &b, const StepK &k, int threads, int minb, int ctas, cudaStream_t stream);
 
 // AoS (reference order, double) <-> SoA conversion
 template <typename R>

@@ -664,6 +664,105 @@ int64_t orc_strand_run(const orc_strand_cfg *cfg, const uint8_t *ctype,
     return nrec;
 }
 
+/* The device AP detector restated in FP64 (see lqt_oracle.h). */
+typedef struct {
+    double vrest, vpeak, dvdt_max, t_act;
+    int phase, ead;
+} orc_det;
+
+enum { DET_IDLE = 0, DET_WAIT = 1, DET_RISE = 2, DET_FALL = 3, DET_DONE = 4 };
+
+int64_t orc_strand_detect(const orc_strand_cfg *cfg, int32_t s1_beats, const uint8_t *ctype, const double *coeff,
+                          const lqt_model *m, double v0, int32_t max_beats, double *t_act, double *apd90,
+                          uint8_t *ead, int32_t *nact, double *final_state)
+{
+    const int n = cfg->n;
+    const double dx = cfg->dx, dt = cfg->dt;
+    double *s = (double *)malloc(sizeof(double) * LQT_NSTATE * n);
+    double *oldV = (double *)malloc(sizeof(double) * n);
+    double *dcoeff = (double *)malloc(sizeof(double) * n);
+    orc_det *det = (orc_det *)calloc(n, sizeof(orc_det));
+    if (!s || !oldV || !dcoeff || !det) {
+        free(s); free(oldV); free(dcoeff); free(det);
+        return -1;
+    }
+    for (int i = 0; i < n; ++i) orc_initial_state(v0, s + i * LQT_NSTATE);
+    for (int i = 0; i < n; ++i) {
+        if (n == 1) dcoeff[i] = 0.0;
+        else if (i == 0) dcoeff[i] = (coeff[i + 1] - coeff[i]) / dx;
+        else if (i == n - 1) dcoeff[i] = (coeff[i] - coeff[i - 1]) / dx;
+        else dcoeff[i] = (coeff[i + 1] - coeff[i - 1]) / (2.0 * dx);
+        nact[i] = 0;
+        ead[i] = 0;
+    }
+    for (int64_t k = 0; k < (int64_t)n * max_beats; ++k) t_act[k] = apd90[k] = -1.0;
+    int prev_on = 0;
+    double time;
+    int64_t step;
+    for (time = 0.0, step = 0; time <= cfg->stop_time; time += dt, step++) {
+        const int on = orc_in_window(time, cfg->bcl, cfg->stim_start, cfg->stim_dur) &&
+                       (s1_beats <= 0 || floor(time / cfg->bcl) < s1_beats);
+        const int opened = on && !prev_on;
+        prev_on = on;
+        for (int i = 0; i < n; ++i) oldV[i] = s[i * LQT_NSTATE + LQT_S_V];
+        for (int i = 0; i < n; ++i) {
+            double ist = (on && i < cfg->n_stim) ? cfg->stim_strength : 0.0;
+            double fo = 0.0, so = 0.0;
+            if (n > 1) {
+                if (i == 0) {
+                    fo = (oldV[1] - oldV[0]) / (1.0 * dx);
+                    so = (oldV[1] + oldV[0] - 2.0 * oldV[0]) / (dx * dx);
+                } else if (i < n - 1) {
+                    fo = (oldV[i + 1] - oldV[i - 1]) / (2.0 * dx);
+                    so = (oldV[i + 1] + oldV[i - 1] - 2.0 * oldV[i]) / (dx * dx);
+                } else {
+                    fo = (oldV[i] - oldV[i - 1]) / (1.0 * dx);
+                    so = (oldV[i] + oldV[i - 1] - 2.0 * oldV[i]) / (dx * dx);
+                }
+            }
+            orc_aux aux;
+            orc_update(s + i * LQT_NSTATE, ctype[i], m, dt, ist, dcoeff[i] * fo + coeff[i] * so, &aux);
+            const double vo = oldV[i], vn = s[i * LQT_NSTATE + LQT_S_V];
+            orc_det *d = &det[i];
+            if (opened) {
+                d->vrest = vo;
+                d->vpeak = vo;
+                d->dvdt_max = 0;
+                d->phase = DET_WAIT;
+                d->ead = 0;
+            }
+            if (d->phase == DET_WAIT) {
+                if (vo < cfg->act_thr && vn >= cfg->act_thr) {
+                    d->phase = DET_RISE;
+                    d->vpeak = vn;
+                    d->t_act = time;
+                    if (nact[i] < max_beats) t_act[(int64_t)i * max_beats + nact[i]] = time;
+                    nact[i]++;
+                }
+            } else if (d->phase == DET_RISE) {
+                if (vn > vo) d->vpeak = vn;
+                else {
+                    d->vpeak = vo;
+                    d->phase = DET_FALL;
+                }
+            } else if (d->phase == DET_FALL) {
+                const double amp = d->vpeak - d->vrest;
+                const double thr90 = d->vpeak - 0.9 * amp, thr50 = d->vpeak - 0.5 * amp;
+                if (vn <= thr90 && vo >= thr90) {
+                    d->phase = DET_DONE;
+                    if (nact[i] - 1 < max_beats) apd90[(int64_t)i * max_beats + nact[i] - 1] = time - d->t_act;
+                    if (d->ead) ead[i] = 1;
+                } else if (vo < thr50 && vn > vo + 1e-3) {
+                    d->ead = 1;
+                }
+            }
+        }
+    }
+    if (final_state) memcpy(final_state, s, sizeof(double) * LQT_NSTATE * n);
+    free(s); free(oldV); free(dcoeff); free(det);
+    return step;
+}
+
 /* PlotScript/plot1DECG_compare.py:89-105 */
 double orc_ecg_1d(int32_t n, const double *v, double dx, double x0)
 {

@@ -79,6 +79,21 @@ int64_t orc_strand_run(const orc_strand_cfg *cfg, const uint8_t *ctype,
                        int64_t rec_cap, int32_t max_beats, double *act,
                        double *cv_out, double *final_state, int nthreads);
 
+/* AP detector per cell and cycle, the definition the device kernels use:
+ * on the step where a cycle's S1 window opens, rest = V before that step; an
+ * upward crossing of act_thr marks activation; the upstroke ends at the first
+ * step whose V is not above the previous V (overshoot = previous V,
+ * SingleCell.cc:160-198); APD90 = time of the first step at or below
+ * overshoot - 0.9 (overshoot - rest) minus the activation time; an EAD is a
+ * rise of more than 1e-3 mV in one step after V fell below the 50% level and
+ * before the 90% crossing.  Outputs per cell: t_act/apd90 per beat
+ * ([n][max_beats], -1 = none), ead flag, beats opened. */
+int64_t orc_strand_detect(const orc_strand_cfg *cfg, int32_t s1_beats,
+                          const uint8_t *ctype, const double *coeff,
+                          const lqt_model *m, double v0, int32_t max_beats,
+                          double *t_act, double *apd90, uint8_t *ead,
+                          int32_t *nact, double *final_state);
+
 /* Pseudo-ECG of a strand (PlotScript/plot1DECG_compare.py:89-105). */
 double orc_ecg_1d(int32_t n, const double *v, double dx, double x0);
 

@@ -100,6 +100,9 @@ def lib():
         L.orc_strand_run.argtypes = [C.POINTER(StrandCfg), P, P, C.POINTER(Model), C.c_double, C.c_int64, P, P,
                                      C.c_int64, C.c_int32, P, P, P, C.c_int]
         L.orc_strand_run.restype = C.c_int64
+        L.orc_strand_detect.argtypes = [C.POINTER(StrandCfg), C.c_int32, P, P, C.POINTER(Model), C.c_double,
+                                        C.c_int32, P, P, P, P, P]
+        L.orc_strand_detect.restype = C.c_int64
         L.orc_ecg_1d.argtypes = [C.c_int32, P, C.c_double, C.c_double]
         L.orc_ecg_1d.restype = C.c_double
         L.orc_build_map.argtypes = [C.c_int32, C.c_int32, C.c_int32, P, P]
@@ -170,6 +173,24 @@ def strand_run(types, coeff, m: Model, *, dx=0.15, dt=0.02, bcl=1000.0, stim_sta
     nrec = lib().orc_strand_run(C.byref(cfg), _p(types), _p(coeff), C.byref(m), v0, rec_every, _p(rec),
                                 _p(rec_t), cap, max_beats, _p(act), _p(cv), _p(fin), nthreads)
     return dict(rec=rec[:nrec], rec_t=rec_t[:nrec], act=act, cv=cv[0], cv_start=cv[1], cv_end=cv[2], final=fin)
+
+
+def strand_detect(types, coeff, m: Model, *, dx=0.15, dt=0.02, bcl=1000.0, stim_start=50.0, stim_dur=1.0,
+                  stim_strength=-52.0, n_stim=3, s1_beats=0, stop_time=2000.0, act_thr=-30.0, v0=-87.5,
+                  max_beats=32):
+    """Single cell (n = 1) or strand run with the device AP detector definition."""
+    types = np.ascontiguousarray(types, dtype=np.uint8)
+    coeff = np.ascontiguousarray(coeff, dtype=np.float64)
+    n = len(types)
+    cfg = StrandCfg(n, dx, dt, bcl, stim_start, stim_dur, stim_strength, n_stim, 0, stop_time, act_thr)
+    t_act = np.zeros((n, max_beats))
+    apd = np.zeros((n, max_beats))
+    ead = np.zeros(n, np.uint8)
+    nact = np.zeros(n, np.int32)
+    fin = np.zeros((n, NSTATE))
+    lib().orc_strand_detect(C.byref(cfg), s1_beats, _p(types), _p(coeff), C.byref(m), v0, max_beats, _p(t_act),
+                            _p(apd), _p(ead), _p(nact), _p(fin))
+    return dict(t_act=t_act, apd90=apd, ead=ead, nact=nact, final=fin)
 
 
 def ecg_1d(v, dx=0.15, x0=35.0):
