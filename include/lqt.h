@@ -336,6 +336,39 @@ int lqt_sim_checkpoint(lqt_sim *s, const char *path);
 int lqt_sim_restore(lqt_sim *s, const char *path);
 
 /* ======================================================================== *
+ *  Learned surrogate network (no counterpart in the reference): MLP
+ *  48 -> 128 -> 128 -> 48 with SiLU, BF16 weights, FP32 accumulation.
+ *  Parameters are one FP32 block of lqt_mlp_num_params() floats:
+ *  W1 [128][48], b1 [128], W2 [128][128], b2 [128], W3 [48][128], b3 [48]
+ *  (weights [out][in]).  Inference runs on the tcgen05 tensor cores with the
+ *  accumulators in TMEM; training (forward, MSE gradient, backward, Adam)
+ *  uses BF16 mma.sync tensor-core GEMMs.  Device buffers belong to the caller.
+ * ======================================================================== */
+typedef struct lqt_mlp lqt_mlp;
+int lqt_mlp_create(uint64_t seed, void *stream, lqt_mlp **out);
+void lqt_mlp_destroy(lqt_mlp *m);
+int64_t lqt_mlp_num_params(void);
+int lqt_mlp_set_params(lqt_mlp *m, const float *params_host);
+/* Parameters and the gradients of the last gradient/training call (NULL skips). */
+int lqt_mlp_get_params(lqt_mlp *m, float *params_host, float *grads_host);
+/* Feature normalisation: x_n = (x - in_mean) * in_scale; state change =
+ * y * out_scale; nvalid = outputs that carry a target (<= 48). */
+int lqt_mlp_set_norm(lqt_mlp *m, const float *in_mean, const float *in_scale,
+                     const float *out_scale, int32_t nvalid);
+/* Shared-memory descriptor stride assignment used by the tensor-core
+ * kernels: 0 = leading offset along K (default), 1 = swapped (diagnostic). */
+int lqt_mlp_set_layout(lqt_mlp *m, int32_t layout);
+/* y[n][48] = MLP(x[n][48]); x BF16, y FP32, both device pointers. */
+int lqt_mlp_infer(lqt_mlp *m, const void *x_bf16_dev, float *y_dev, int64_t n);
+/* Loss = mean over the nvalid outputs of (y - t)^2 and its gradients for a
+ * batch (multiple of 16) of device inputs (BF16) and targets (FP32). */
+int lqt_mlp_gradients(lqt_mlp *m, const void *x_bf16_dev, const float *t_dev,
+                      int64_t batch, double *loss);
+/* lqt_mlp_gradients followed by one Adam step (beta 0.9 / 0.999). */
+int lqt_mlp_train_step(lqt_mlp *m, const void *x_bf16_dev, const float *t_dev,
+                       int64_t batch, float lr, double *loss);
+
+/* ======================================================================== *
  *  Synthetic geometries (seeded).  The reference reads its geometry from
  *  files that are not distributed (wholeventriclewithfibervector.txt,
  *  157layerwithfibervector.txt, GPU3D.cu:1276, new_11.cu:1296); these
