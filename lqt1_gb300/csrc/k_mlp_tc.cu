@@ -72,7 +72,10 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer_tc(const __nv_bfloat16 *__
     stage_kmajor(smem + kOffW1, w.w1t, kMlpHid, kMlpIn);
     stage_kmajor(smem + kOffW2, w.w2t, kMlpHid, kMlpHid);
     stage_kmajor(smem + kOffW3, w.w3t, kMlpOut, kMlpHid);
-    if (tid == 0) tc::mbar_init(bar, 1);
+    if (tid == 0) {
+        tc::mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
     if (warp == 0) tc::tmem_alloc(tslot, kTmemCols);
     tc::fence_before();
     __syncthreads();
@@ -172,7 +175,8 @@ cudaError_t launch_mlp_infer_tc(const __nv_bfloat16 *X, float *Y, const MlpDev &
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const int64_t ntiles = (n + kTile - 1) / kTile;
-    // at most 2 CTAs per SM (2 x 256 TMEM columns = the SM's 512)
+    // at most 2 CTAs per SM (shared memory admits 2; 2 x 256 TMEM columns =
+    // the SM's 512), so tcgen05.alloc never waits for another CTA
     const int64_t grid = ntiles < 2LL * nsm ? ntiles : 2LL * nsm;
     k_mlp_infer_tc<<<(unsigned)grid, 128, kSmemBytes, st>>>(X, Y, w, n, err, swap);
     return cudaGetLastError();
