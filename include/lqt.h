@@ -368,6 +368,29 @@ int lqt_mlp_gradients(lqt_mlp *m, const void *x_bf16_dev, const float *t_dev,
 int lqt_mlp_train_step(lqt_mlp *m, const void *x_bf16_dev, const float *t_dev,
                        int64_t batch, float lr, double *loss);
 
+/* Training pairs for the surrogate from the plain mixed-form integrator:
+ * ncells paced cells with seeded uniform parameters in the given ranges
+ * (GKs factor, PCa factor, GKs-ISO factor, BCL; type uniform over
+ * endo/M/epi; 2 ms x -52 pA/pF at 50 ms of each cycle).  After beats_warm
+ * cycles, at macro-step boundaries where |dV/dt| <= dvdt_max and no stimulus
+ * falls in the next 0.1 ms, each cell records with probability prob:
+ * x_dev[row][44] = 38 states (V, 8 concentrations, 29 gates) + 3 factors +
+ * endo/epi/M one-hot, d_dev[row][38] = their change over 0.1 ms.  Up to cap
+ * rows; *count = rows written. */
+typedef struct lqt_sur_ranges {
+    double gks[2], pca[2], iso[2], bcl[2];
+    int32_t beats_warm, beats_record;
+    double dt, dvdt_max, prob;
+} lqt_sur_ranges;
+int lqt_sur_datagen(int64_t ncells, uint64_t seed, const lqt_sur_ranges *ranges,
+                    float *x_dev, float *d_dev, int64_t cap, int64_t *count,
+                    void *stream);
+/* Rows idx_dev[n] (or 0..n-1 when NULL) of raw features / changes -> the
+ * network's normalised BF16 inputs xb_dev[n][48] and FP32 targets t_dev[n][48]
+ * (d_dev may be NULL for inputs only). */
+int lqt_sur_prepare(lqt_mlp *m, const float *x_dev, const float *d_dev,
+                    const int64_t *idx_dev, int64_t n, void *xb_dev, float *t_dev);
+
 /* ======================================================================== *
  *  Synthetic geometries (seeded).  The reference reads its geometry from
  *  files that are not distributed (wholeventriclewithfibervector.txt,

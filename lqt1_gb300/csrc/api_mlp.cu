@@ -260,3 +260,72 @@ int lqt_mlp_train_step(lqt_mlp *m, const void *x_bf16_dev, const float *t_dev, i
 }
 
 }  // extern "C"
+
+// ---- training data ------------------------------------------------------------
+#include "sur.h"
+
+extern "C" {
+
+int lqt_sur_datagen(int64_t ncells, uint64_t seed, const lqt_sur_ranges *r, float *x_dev, float *d_dev, int64_t cap,
+                    int64_t *count, void *stream)
+{
+    if (ncells <= 0 || !r || !x_dev || !d_dev || cap <= 0 || !count)
+        return fail(LQT_ERR_INVALID, "lqt_sur_datagen: bad arguments");
+    if (!(r->bcl[0] > 10) || r->bcl[1] < r->bcl[0] || r->beats_warm < 0 || r->beats_record < 1 || !(r->dt > 0) ||
+        !(r->prob > 0) || r->prob > 1)
+        return fail(LQT_ERR_INVALID, "lqt_sur_datagen: ranges (bcl > 10, beats_record >= 1, 0 < prob <= 1, dt > 0)");
+    std::mt19937_64 rng(seed);
+    std::uniform_real_distribution<double> U(0.0, 1.0);
+    std::vector<SurCell> cells(ncells);
+    std::vector<ModelK> models(ncells);
+    for (int64_t i = 0; i < ncells; ++i) {
+        lqt_model mm{};
+        mm.pca_scale = r->pca[0] + (r->pca[1] - r->pca[0]) * U(rng);
+        mm.gks_scale = r->gks[0] + (r->gks[1] - r->gks[0]) * U(rng);
+        mm.gks_iso_scale = r->iso[0] + (r->iso[1] - r->iso[0]) * U(rng);
+        models[i] = make_modelk(mm);
+        const double bcl = r->bcl[0] + (r->bcl[1] - r->bcl[0]) * U(rng);
+        SurCell &c = cells[i];
+        c.bcl_steps = (int64_t)std::llround(bcl / r->dt);
+        c.warm_steps = c.bcl_steps * r->beats_warm;
+        c.nsteps = c.bcl_steps * (r->beats_warm + r->beats_record);
+        c.stim_on = (int64_t)std::llround(50.0 / r->dt);
+        c.stim_off = c.stim_on + (int64_t)std::llround(2.0 / r->dt);
+        c.model = (int32_t)i;
+        const double u = U(rng);
+        c.ctype = u < 1.0 / 3 ? LQT_ENDO : (u < 2.0 / 3 ? LQT_MCELL : LQT_EPI);
+        c.stim = -52.f;
+        c.gks_scale = (float)mm.gks_scale;
+        c.pca_scale = (float)mm.pca_scale;
+        c.iso_scale = (float)mm.gks_iso_scale;
+    }
+    DevMem tmp;
+    SurCell *dc = nullptr;
+    ModelK *dm = nullptr;
+    unsigned long long *cnt = nullptr;
+    if (tmp.alloc((void **)&dc, ncells * sizeof(SurCell)) | tmp.alloc((void **)&dm, ncells * sizeof(ModelK)) |
+        tmp.alloc((void **)&cnt, 16))
+        return LQT_ERR_NOMEM;
+    cudaStream_t st = (cudaStream_t)stream;
+    CK(cudaMemcpyAsync(dc, cells.data(), ncells * sizeof(SurCell), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dm, models.data(), ncells * sizeof(ModelK), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(cnt, 0, 8, st));
+    CK(launch_sur_datagen(dc, ncells, dm, make_stepk(r->dt), x_dev, d_dev, cnt, cap, seed, (float)r->dvdt_max,
+                          (float)r->prob, st));
+    unsigned long long c = 0;
+    CK(cudaMemcpyAsync(&c, cnt, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    *count = (int64_t)std::min<unsigned long long>(c, (unsigned long long)cap);
+    return LQT_OK;
+}
+
+int lqt_sur_prepare(lqt_mlp *m, const float *x_dev, const float *d_dev, const int64_t *idx_dev, int64_t n,
+                    void *xb_dev, float *t_dev)
+{
+    if (!m || !x_dev || !xb_dev || n < 0) return fail(LQT_ERR_INVALID, "lqt_sur_prepare: bad arguments");
+    CK(launch_sur_prepare(x_dev, d_dev, idx_dev, n, m->norm, (__nv_bfloat16 *)xb_dev, d_dev ? t_dev : nullptr,
+                          m->stream));
+    return LQT_OK;
+}
+
+}  // extern "C"

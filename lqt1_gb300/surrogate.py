@@ -69,6 +69,7 @@ class Mlp:
 
     def set_norm(self, in_mean, in_scale, out_scale, nvalid=N_STATE):
         a = [np.ascontiguousarray(x, np.float32) for x in (in_mean, in_scale, out_scale)]
+        self.norm_in_mean, self.norm_in_scale, self.norm_out = a
         N.check(self.L.lqt_mlp_set_norm(self._h, a[0].ctypes.data, a[1].ctypes.data, a[2].ctypes.data, nvalid),
                 "lqt_mlp_set_norm")
 
@@ -90,3 +91,107 @@ class Mlp:
         N.check(self.L.lqt_mlp_train_step(self._h, x_bf16.data_ptr(), t_f32.data_ptr(), x_bf16.shape[0], lr,
                                           C.byref(loss)), "lqt_mlp_train_step")
         return loss.value
+
+
+class SurRanges(C.Structure):
+    _fields_ = [("gks", C.c_double * 2), ("pca", C.c_double * 2), ("iso", C.c_double * 2), ("bcl", C.c_double * 2),
+                ("beats_warm", C.c_int32), ("beats_record", C.c_int32), ("dt", C.c_double), ("dvdt_max", C.c_double),
+                ("prob", C.c_double)]
+
+
+def _bind_sur():
+    L = _bind()
+    P = C.c_void_p
+    L.lqt_sur_datagen.argtypes = [C.c_int64, C.c_uint64, C.POINTER(SurRanges), P, P, C.c_int64,
+                                  C.POINTER(C.c_int64), P]
+    L.lqt_sur_datagen.restype = C.c_int
+    L.lqt_sur_prepare.argtypes = [P, P, P, P, C.c_int64, P, P]
+    L.lqt_sur_prepare.restype = C.c_int
+    return L
+
+
+def generate(ncells=65536, seed=1, cap=20_000_000, *, gks=(0.05, 1.0), pca=(1.0, 2.2), iso=(1.0, 2.0),
+             bcl=(400.0, 2000.0), beats_warm=3, beats_record=6, dvdt_max=2.0, prob=0.05, dt=0.02, stream=None):
+    """Training pairs from the plain mixed-form integrator on the GPU.
+    Returns torch tensors X [n, 44] (raw features) and D [n, 38] (changes over 0.1 ms)."""
+    import torch
+    L = _bind_sur()
+    X = torch.empty((cap, 44), dtype=torch.float32, device="cuda")
+    D = torch.empty((cap, N_STATE), dtype=torch.float32, device="cuda")
+    r = SurRanges((C.c_double * 2)(*gks), (C.c_double * 2)(*pca), (C.c_double * 2)(*iso), (C.c_double * 2)(*bcl),
+                  beats_warm, beats_record, dt, dvdt_max, prob)
+    n = C.c_int64()
+    N.check(L.lqt_sur_datagen(ncells, seed, C.byref(r), X.data_ptr(), D.data_ptr(), cap, C.byref(n),
+                              C.c_void_p(stream or 0)), "lqt_sur_datagen")
+    return X[:n.value], D[:n.value]
+
+
+def fit_norm(X, D, nsample=500_000, seed=0):
+    """Per-feature normalisation from a sample: inputs to zero mean / unit std
+    (constant features keep scale 1), targets divided by their std."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    idx = torch.randint(0, X.shape[0], (min(nsample, X.shape[0]),), device="cuda", generator=g)
+    xs = X[idx].double().cpu().numpy()
+    ds = D[idx].double().cpu().numpy()
+    in_mean = np.zeros(IN, np.float32)
+    in_scale = np.ones(IN, np.float32)
+    mu, sd = xs.mean(0), xs.std(0)
+    in_mean[:44] = mu
+    in_scale[:44] = np.where(sd > 1e-12 * np.maximum(1.0, np.abs(mu)), 1.0 / np.maximum(sd, 1e-30), 1.0)
+    out_scale = np.ones(OUT, np.float32)
+    out_scale[:N_STATE] = np.maximum(ds.std(0), 1e-12)
+    return in_mean, in_scale, out_scale
+
+
+def train(mlp: Mlp, X, D, *, epochs=4, batch=8192, lr=2e-3, lr_min=1e-4, holdout=0.01, seed=0, log_every=500,
+          log=print):
+    """Adam on shuffled mini-batches with a cosine learning-rate schedule.
+    Returns per-state validation RMSE (physical units) and the loss history."""
+    import math
+
+    import torch
+    L = _bind_sur()
+    n = X.shape[0]
+    nval = max(batch, int(n * holdout)) // 16 * 16
+    ntr = n - nval
+    xb = torch.empty((batch, IN), dtype=torch.bfloat16, device="cuda")
+    t = torch.empty((batch, OUT), dtype=torch.float32, device="cuda")
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    steps = epochs * (ntr // batch)
+    hist = []
+    k = 0
+    for ep in range(epochs):
+        perm = torch.randperm(ntr, device="cuda", generator=g)
+        for b in range(ntr // batch):
+            idx = perm[b * batch:(b + 1) * batch]
+            N.check(L.lqt_sur_prepare(mlp._h, X.data_ptr(), D.data_ptr(), idx.data_ptr(), batch, xb.data_ptr(),
+                                      t.data_ptr()), "lqt_sur_prepare")
+            cur = lr_min + 0.5 * (lr - lr_min) * (1 + math.cos(math.pi * k / max(1, steps)))
+            if k % log_every == 0 or k == steps - 1:
+                loss = mlp.train_step(xb, t, cur)
+                hist.append((k, loss))
+                log(f"step {k}/{steps} lr {cur:.2e} loss {loss:.3e}")
+            else:
+                N.check(mlp.L.lqt_mlp_train_step(mlp._h, xb.data_ptr(), t.data_ptr(), batch, cur, None),
+                        "lqt_mlp_train_step")
+            k += 1
+    return validate(mlp, X[ntr:], D[ntr:]), hist
+
+
+def validate(mlp: Mlp, Xv, Dv, out_scale=None):
+    """Per-state RMSE of the predicted change over 0.1 ms (physical units) and
+    the RMSE of the zero-change baseline, on tcgen05 inference."""
+    import torch
+    L = _bind_sur()
+    n = Xv.shape[0]
+    xb = torch.empty((n, IN), dtype=torch.bfloat16, device="cuda")
+    y = torch.empty((n, OUT), dtype=torch.float32, device="cuda")
+    N.check(L.lqt_sur_prepare(mlp._h, Xv.data_ptr(), None, None, n, xb.data_ptr(), None), "lqt_sur_prepare")
+    mlp.infer(xb, y)
+    os_ = mlp.norm_out if out_scale is None else out_scale
+    pred = y[:, :N_STATE].double().cpu().numpy() * os_[:N_STATE]
+    true = Dv.double().cpu().numpy()
+    rmse = np.sqrt(((pred - true) ** 2).mean(0))
+    base = np.sqrt((true ** 2).mean(0))
+    return dict(rmse=rmse, zero_rmse=base, n=n)
