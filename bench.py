@@ -261,7 +261,7 @@ def main():
     nbad = sim.check()
 
     # roofline of the dominant kernel: per-launch CUDA-event time of k_grid_step
-    ms_step, ms_ghost = sim.profile(20)
+    ms_step, ms_ghost, _ = sim.profile(20)
     peaks = measured_peaks()
     peak = peaks.get("hbm_gbs")
     peak_kind = "measured" if peak else "fallback"
@@ -305,7 +305,7 @@ def main():
         b.record(stream)
         torch.cuda.synchronize()
         v64 = n * args.fp64_steps / (a.elapsed_time(b) / 1e3)
-        ms64, _ = s64.profile(2)
+        ms64, _, _ = s64.profile(2)
         fp64 = {"value": v64 * world, "unit": UNIT, "steps": args.fp64_steps, "kernel_ms": ms64,
                 "achieved_gbs": BYTES_FP64 * n / (ms64 / 1e3) / 1e9, "mixed_over_fp64": value / (v64 * world)}
         s64.close()

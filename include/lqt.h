@@ -283,9 +283,13 @@ int lqt_sim_get_ecg(lqt_sim *s, int64_t max_samples, double *phi_host,
 
 /* Detector results per tissue voxel (detect = 1): last activation time (ms,
  * first upward crossing of act_threshold in a cycle, OneD.cc:419-436), APD90
- * of the last completed beat (ms from activation; amplitude rule of
- * SingleCell.cc:185-212) and an EAD flag (second upstroke above -60 mV before
- * 90% repolarisation).  NULL pointers are skipped. */
+ * of the last completed beat (ms from activation to the first step at or
+ * below overshoot - 0.9 * (overshoot - rest), the amplitude rule of
+ * SingleCell.cc:185-212, with the overshoot taken as the maximum V since
+ * activation: in tissue an upstroke can stall for one step where waves
+ * collide, and the single-cell "first non-rising step" would then depend on
+ * microvolt differences) and an EAD flag (a rise of V after the 50% level,
+ * before 90% repolarisation).  NULL pointers are skipped. */
 int lqt_sim_get_detect(lqt_sim *s, float *t_act_host, float *apd90_host,
                        uint8_t *ead_host);
 
@@ -299,9 +303,12 @@ int lqt_sim_tune(lqt_sim *s, int32_t variant, int32_t *chosen, float *ms_per_var
 
 /* Instrumentation (no counterpart in the reference, which has no timing):
  * run nsteps steps without graph capture, timing each launch of the fused
- * step kernel and of the ghost/clock kernel with CUDA events on the
- * simulation's stream; returns the mean milliseconds per launch. */
-int lqt_sim_profile(lqt_sim *s, int64_t nsteps, double *ms_step, double *ms_ghost);
+ * step kernel, of the ghost/clock kernel and (with a surrogate attached) of
+ * the surrogate macro-step kernel with CUDA events on the simulation's
+ * stream; returns the mean milliseconds per launch (ms_sur: per macro-step
+ * launch, 0 when none ran).  NULL outputs are skipped. */
+int lqt_sim_profile(lqt_sim *s, int64_t nsteps, double *ms_step, double *ms_ghost,
+                    double *ms_sur);
 
 /* Mirror-boundary map (GPU3D.cu:1487-1604): the empty grid voxels next to
  * tissue and, for each, the grid index of the tissue voxel whose V it holds.
@@ -355,6 +362,11 @@ int lqt_mlp_get_params(lqt_mlp *m, float *params_host, float *grads_host);
  * y * out_scale; nvalid = outputs that carry a target (<= 48). */
 int lqt_mlp_set_norm(lqt_mlp *m, const float *in_mean, const float *in_scale,
                      const float *out_scale, int32_t nvalid);
+/* Residual bounds of the surrogate (48 values > 0, normalised output units):
+ * a tissue macro step accepts a voxel only if every normalised correction
+ * |y_j| <= kappa * out_bound[j] (lqt_sur_config.kappa); typically the largest
+ * |target| of the training set.  Default: unbounded. */
+int lqt_mlp_set_bounds(lqt_mlp *m, const float *out_bound);
 /* Shared-memory descriptor stride assignment used by the tensor-core
  * kernels: 0 = leading offset along K (default), 1 = swapped (diagnostic). */
 int lqt_mlp_set_layout(lqt_mlp *m, int32_t layout);
@@ -375,12 +387,16 @@ int lqt_mlp_train_step(lqt_mlp *m, const void *x_bf16_dev, const float *t_dev,
  * cycles, at macro-step boundaries where |dV/dt| <= dvdt_max and no stimulus
  * falls in the next 0.1 ms, each cell records with probability prob:
  * x_dev[row][44] = 38 states (V, 8 concentrations, 29 gates) + 3 factors +
- * endo/epi/M one-hot, d_dev[row][38] = their change over 0.1 ms.  Up to cap
- * rows; *count = rows written. */
+ * endo/epi/M one-hot, d_dev[row][38] = the state after 5 plain steps of
+ * 0.02 ms minus the state after one coarse step of 0.1 ms from the same
+ * start (the correction the network learns).  Macro steps that are not
+ * recorded carry a seeded constant current uniform in +-jitter pA/pF, which
+ * moves the cells off the single-cell trajectory as tissue coupling does.
+ * Up to cap rows; *count = rows written. */
 typedef struct lqt_sur_ranges {
     double gks[2], pca[2], iso[2], bcl[2];
     int32_t beats_warm, beats_record;
-    double dt, dvdt_max, prob;
+    double dt, dvdt_max, prob, jitter;
 } lqt_sur_ranges;
 int lqt_sur_datagen(int64_t ncells, uint64_t seed, const lqt_sur_ranges *ranges,
                     float *x_dev, float *d_dev, int64_t cap, int64_t *count,
@@ -390,6 +406,35 @@ int lqt_sur_datagen(int64_t ncells, uint64_t seed, const lqt_sur_ranges *ranges,
  * (d_dev may be NULL for inputs only). */
 int lqt_sur_prepare(lqt_mlp *m, const float *x_dev, const float *d_dev,
                     const int64_t *idx_dev, int64_t n, void *xb_dev, float *t_dev);
+
+/* The surrogate inside a tissue simulation (mixed form only).  Every 5
+ * steps (steps whose index is a multiple of 5) one kernel offers each tissue
+ * voxel whose |dV/dt| over the last step is at most dvdt_max, and that no
+ * stimulus reaches in the next 5 steps, to the surrogate: one coarse TPORd
+ * step of 5 dt plus the network's correction (use_net = 1; 0 = the coarse
+ * step alone).  The residual check (every normalised correction within
+ * +-kappa times its bound, lqt_mlp_set_bounds; gates within [0, 1];
+ * concentrations positive; ionic V change of the macro step within
+ * +-vstep_max mV) decides per voxel; a voxel that
+ * passes keeps its new ionic state and, for the next 5 steps, moves V by the
+ * macro step's ionic rate plus diffusion only.  Every other voxel runs the
+ * plain step.  The network must be trained for this dt (training pairs from
+ * lqt_sur_datagen with the same dt).  m = NULL detaches.  m stays owned by
+ * the caller and must outlive the attachment; its parameters are read at
+ * every macro step. */
+typedef struct lqt_sur_config {
+    double dvdt_max;    /* mV/ms, e.g. 1 */
+    double kappa;       /* multiplier of the network's residual bounds, e.g. 1.5 */
+    double vstep_max;   /* mV per macro step, e.g. 0.3 */
+    int32_t use_net;
+    int32_t reserved;   /* must be zero */
+} lqt_sur_config;
+int lqt_sim_set_surrogate(lqt_sim *s, lqt_mlp *m, const lqt_sur_config *cfg);
+/* Counters since the last reset: macro steps launched, voxel offers, voxels
+ * accepted; wait_timeouts = 1 if a tensor-core completion wait ran out (the
+ * affected voxels ran the plain step).  reset != 0 zeroes them. */
+int lqt_sim_surrogate_stats(lqt_sim *s, int64_t *macro_steps, int64_t *offered,
+                            int64_t *accepted, int32_t *wait_timeouts, int32_t reset);
 
 /* ======================================================================== *
  *  Synthetic geometries (seeded).  The reference reads its geometry from

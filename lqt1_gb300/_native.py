@@ -64,6 +64,11 @@ class SimParams(C.Structure):
 _lib = None
 
 
+class SurConfig(C.Structure):
+    _fields_ = [("dvdt_max", C.c_double), ("kappa", C.c_double), ("vstep_max", C.c_double), ("use_net", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
 def lib():
     """Load liblqt.so (building it first if this checkout has no build yet)."""
     global _lib

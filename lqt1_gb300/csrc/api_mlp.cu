@@ -36,7 +36,7 @@ struct lqt_mlp {
     DevMem mem;
     float *P = nullptr, *G = nullptr, *M = nullptr, *V = nullptr;
     __nv_bfloat16 *Pb = nullptr;
-    float *norm = nullptr;          // in_mean[48], in_scale[48], out_scale[48]
+    float *norm = nullptr;          // in_mean[48], in_scale[48], out_scale[48], out_bound[48]
     int *err = nullptr;
     double *loss = nullptr;
     int64_t adam_t = 0;
@@ -52,6 +52,16 @@ struct lqt_mlp {
         return MlpDev{Pb + kOW1, Pb + kOW2, Pb + kOW3, P + kOB1, P + kOB2, P + kOB3};
     }
 };
+
+namespace lqt {
+bool mlp_device_view(const lqt_mlp *m, MlpDev *w, const float **norm)
+{
+    if (!m || !m->P || !m->Pb || !m->norm) return false;
+    *w = m->dev();
+    *norm = m->norm;
+    return true;
+}
+}  // namespace lqt
 
 static int upload_params(lqt_mlp *m, const std::vector<float> &p)
 {
@@ -148,7 +158,7 @@ int lqt_mlp_create(uint64_t seed, void *stream, lqt_mlp **out)
     m->stream = (cudaStream_t)stream;
     int rc = m->mem.alloc((void **)&m->P, kNParam * 4) | m->mem.alloc((void **)&m->G, kNParam * 4) |
              m->mem.alloc((void **)&m->M, kNParam * 4) | m->mem.alloc((void **)&m->V, kNParam * 4) |
-             m->mem.alloc((void **)&m->Pb, kNParam * 2) | m->mem.alloc((void **)&m->norm, 3 * kMlpIn * 4) |
+             m->mem.alloc((void **)&m->Pb, kNParam * 2) | m->mem.alloc((void **)&m->norm, 4 * kMlpIn * 4) |
              m->mem.alloc((void **)&m->err, 16) | m->mem.alloc((void **)&m->loss, 16);
     if (rc) {
         delete m;
@@ -162,8 +172,11 @@ int lqt_mlp_create(uint64_t seed, void *stream, lqt_mlp **out)
     for (int64_t i = 0; i < kMlpHid * kMlpHid; ++i) p[kOW2 + i] = N01(rng) * std::sqrt(2.f / kMlpHid);
     for (int64_t i = 0; i < kMlpOut * kMlpHid; ++i) p[kOW3 + i] = N01(rng) * std::sqrt(1.f / kMlpHid);
     rc = upload_params(m, p);
-    std::vector<float> nrm(3 * kMlpIn, 0.f);
-    for (int i = 0; i < kMlpIn; ++i) nrm[kMlpIn + i] = nrm[2 * kMlpIn + i] = 1.f;
+    std::vector<float> nrm(4 * kMlpIn, 0.f);
+    for (int i = 0; i < kMlpIn; ++i) {
+        nrm[kMlpIn + i] = nrm[2 * kMlpIn + i] = 1.f;
+        nrm[3 * kMlpIn + i] = INFINITY;       // no residual bound until one is set
+    }
     if (!rc && cudaMemcpy(m->norm, nrm.data(), nrm.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)
         rc = LQT_ERR_CUDA;
     if (!rc && cudaMemset(m->err, 0, 16) != cudaSuccess) rc = LQT_ERR_CUDA;
@@ -207,6 +220,15 @@ int lqt_mlp_set_norm(lqt_mlp *m, const float *in_mean, const float *in_scale, co
     std::memcpy(v.data() + 2 * kMlpIn, out_scale, kMlpOut * 4);
     CK(cudaMemcpy(m->norm, v.data(), v.size() * 4, cudaMemcpyHostToDevice));
     m->nvalid = nvalid;
+    return LQT_OK;
+}
+
+int lqt_mlp_set_bounds(lqt_mlp *m, const float *out_bound)
+{
+    if (!m || !out_bound) return fail(LQT_ERR_INVALID, "lqt_mlp_set_bounds: NULL");
+    for (int i = 0; i < kMlpOut; ++i)
+        if (!(out_bound[i] > 0)) return fail(LQT_ERR_INVALID, "lqt_mlp_set_bounds: bounds must be > 0");
+    CK(cudaMemcpy(m->norm + 3 * kMlpIn, out_bound, kMlpOut * 4, cudaMemcpyHostToDevice));
     return LQT_OK;
 }
 
@@ -272,8 +294,8 @@ int lqt_sur_datagen(int64_t ncells, uint64_t seed, const lqt_sur_ranges *r, floa
     if (ncells <= 0 || !r || !x_dev || !d_dev || cap <= 0 || !count)
         return fail(LQT_ERR_INVALID, "lqt_sur_datagen: bad arguments");
     if (!(r->bcl[0] > 10) || r->bcl[1] < r->bcl[0] || r->beats_warm < 0 || r->beats_record < 1 || !(r->dt > 0) ||
-        !(r->prob > 0) || r->prob > 1)
-        return fail(LQT_ERR_INVALID, "lqt_sur_datagen: ranges (bcl > 10, beats_record >= 1, 0 < prob <= 1, dt > 0)");
+        !(r->prob > 0) || r->prob > 1 || !(r->jitter >= 0))
+        return fail(LQT_ERR_INVALID, "lqt_sur_datagen: ranges (bcl > 10, beats_record >= 1, 0 < prob <= 1, dt > 0, jitter >= 0)");
     std::mt19937_64 rng(seed);
     std::uniform_real_distribution<double> U(0.0, 1.0);
     std::vector<SurCell> cells(ncells);
@@ -310,8 +332,8 @@ int lqt_sur_datagen(int64_t ncells, uint64_t seed, const lqt_sur_ranges *r, floa
     CK(cudaMemcpyAsync(dc, cells.data(), ncells * sizeof(SurCell), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(dm, models.data(), ncells * sizeof(ModelK), cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(cnt, 0, 8, st));
-    CK(launch_sur_datagen(dc, ncells, dm, make_stepk(r->dt), x_dev, d_dev, cnt, cap, seed, (float)r->dvdt_max,
-                          (float)r->prob, st));
+    CK(launch_sur_datagen(dc, ncells, dm, make_stepk(r->dt), make_stepk(kSurSteps * r->dt), x_dev, d_dev, cnt, cap,
+                          seed, (float)r->dvdt_max, (float)r->prob, (float)r->jitter, st));
     unsigned long long c = 0;
     CK(cudaMemcpyAsync(&c, cnt, 8, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));

@@ -19,11 +19,14 @@
 #include "api_common.h"
 #include "geometry.h"
 #include "grid_dev.h"
+#include "sur.h"
 
 using namespace lqt;
 
 namespace {
-constexpr int kGraphChunk = 50;   // steps per captured graph (even: V buffer parity is kept)
+constexpr int kGraphChunk = 50;   // steps per captured graph (even: V buffer parity is kept;
+                                  // a multiple of the surrogate's macro step)
+static_assert(kGraphChunk % kSurSteps == 0, "graph chunks must start on macro-step boundaries");
 constexpr uint32_t kCkptMagic = 0x4c515443;   // "LQTC"
 constexpr uint32_t kCkptVersion = 1;
 }  // namespace
@@ -71,6 +74,16 @@ struct lqt_sim {
     int minb = 2;
     bool tuned = false;
     float tune_ms[4] = {0, 0, 0, 0};
+    // learned surrogate (mixed form): network, per-voxel rate, counters
+    lqt_mlp *sur = nullptr;
+    lqt_sur_config sur_cfg{};
+    float *srate = nullptr;
+    int32_t *plist = nullptr;
+    unsigned long long *plist_n = nullptr;
+    bool plist_valid = false;       // rate/list written by a macro-step launch still in effect
+    unsigned long long *sur_stats = nullptr;
+    int *sur_err = nullptr;
+    int64_t sur_launches = 0;
     // graph
     cudaGraphExec_t graph = nullptr;
     int graph_cur = -1;
@@ -126,6 +139,10 @@ struct lqt_sim {
         g.vmin_ok = (R)p.vmin_ok;
         g.vmax_ok = (R)p.vmax_ok;
         g.nbad = nbad;
+        const bool in_macro = sur && plist_valid;
+        g.srate = in_macro ? srate : nullptr;
+        g.plist = in_macro ? plist : nullptr;
+        g.plist_n = in_macro ? (const int64_t *)plist_n : nullptr;
         return g;
     }
     double diso = 0.154;
@@ -199,18 +216,60 @@ int refresh_windows(lqt_sim *s, int64_t horizon)
     return LQT_OK;
 }
 
-int launch_step(lqt_sim *s)
+// At a macro-step boundary with a surrogate attached: the macro-step kernel.
+int launch_sur_if_due(lqt_sim *s)
+{
+    if (!s->sur || s->step % kSurSteps != 0) return LQT_OK;
+    SurGrid sg{};
+    if (!mlp_device_view(s->sur, &sg.w, &sg.norm)) return fail(LQT_ERR_STATE, "surrogate network has no parameters");
+    sg.rate = s->srate;
+    sg.plist = s->plist;
+    sg.plist_n = s->plist_n;
+    sg.stats = s->sur_stats;
+    sg.err = s->sur_err;
+    sg.kmac = step_as<float>(make_stepk(kSurSteps * s->p.dt));
+    sg.par[0] = (float)s->p.model.gks_scale;
+    sg.par[1] = (float)s->p.model.pca_scale;
+    sg.par[2] = (float)s->p.model.gks_iso_scale;
+    sg.dvdt_max = (float)s->sur_cfg.dvdt_max;
+    sg.kappa = (float)s->sur_cfg.kappa;
+    sg.vstep_max = (float)s->sur_cfg.vstep_max;
+    sg.nsub = kSurSteps;
+    sg.use_net = s->sur_cfg.use_net;
+    CK(cudaMemsetAsync(s->plist_n, 0, sizeof(unsigned long long), s->stream));
+    CK(launch_sur_grid(devf<float>(s), sg, s->cur, s->dim, s->stream));
+    s->sur_launches += 1;
+    s->plist_valid = true;
+    return LQT_OK;
+}
+
+// The step kernels of one step (without the ghost refresh): the fused plain
+// step over all voxels, or, inside a surrogate macro step, the V-only step of
+// the surrogate voxels and the plain step over the listed ones.
+cudaError_t launch_substep(lqt_sim *s)
 {
     const StepK k = make_stepk(s->p.dt);
-    if (s->fp64()) {
-        const GridDev<double> g = devf<double>(s);
-        CK(launch_grid_step<double>(g, k, s->cur, s->dim, s->minb, s->stream));
-        CK(launch_ghost<double>(g, s->cur ^ 1, s->stream));
-    } else {
-        const GridDev<float> g = devf<float>(s);
-        CK(launch_grid_step<float>(g, k, s->cur, s->dim, s->minb, s->stream));
-        CK(launch_ghost<float>(g, s->cur ^ 1, s->stream));
+    if (s->fp64()) return launch_grid_step<double>(devf<double>(s), k, s->cur, s->dim, s->minb, s->stream);
+    const GridDev<float> g = devf<float>(s);
+    if (g.srate) {
+        cudaError_t e = launch_sur_substep(g, s->p.dt, s->cur, s->dim, s->stream);
+        if (e != cudaSuccess) return e;
     }
+    return launch_grid_step<float>(g, k, s->cur, s->dim, s->minb, s->stream);
+}
+
+cudaError_t launch_ghost_now(lqt_sim *s)
+{
+    return s->fp64() ? launch_ghost<double>(devf<double>(s), s->cur ^ 1, s->stream)
+                     : launch_ghost<float>(devf<float>(s), s->cur ^ 1, s->stream);
+}
+
+int launch_step(lqt_sim *s)
+{
+    int rc = launch_sur_if_due(s);
+    if (rc) return rc;
+    CK(launch_substep(s));
+    CK(launch_ghost_now(s));
     s->cur ^= 1;
     return LQT_OK;
 }
@@ -256,15 +315,12 @@ int autotune(lqt_sim *s, int per, int64_t *consumed)
         s->minb = cand[c];
         float tot = 0.f;
         for (int i = 0; i < per && rc == LQT_OK; ++i) {
+            rc = launch_sur_if_due(s);
+            if (rc) break;
             cudaError_t e = cudaEventRecord(a, s->stream);
-            const StepK k = make_stepk(s->p.dt);
-            if (e == cudaSuccess)
-                e = s->fp64() ? launch_grid_step<double>(devf<double>(s), k, s->cur, s->dim, s->minb, s->stream)
-                              : launch_grid_step<float>(devf<float>(s), k, s->cur, s->dim, s->minb, s->stream);
+            if (e == cudaSuccess) e = launch_substep(s);
             if (e == cudaSuccess) e = cudaEventRecord(b, s->stream);
-            if (e == cudaSuccess)
-                e = s->fp64() ? launch_ghost<double>(devf<double>(s), s->cur ^ 1, s->stream)
-                              : launch_ghost<float>(devf<float>(s), s->cur ^ 1, s->stream);
+            if (e == cudaSuccess) e = launch_ghost_now(s);
             if (e == cudaSuccess) e = cudaEventSynchronize(b);
             float ms = 0.f;
             if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
@@ -308,8 +364,12 @@ int build_graph(lqt_sim *s)
     int rc = LQT_OK;
     // capture with step numbers aligned to the ECG cadence: the graph is
     // replayed only from steps that are multiples of kGraphChunk
+    const int64_t launches0 = s->sur_launches;
+    const bool plist0 = s->plist_valid;
     for (int i = 0; i < kGraphChunk && rc == LQT_OK; ++i) rc = step_once(s);
     cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+    s->sur_launches = launches0;
+    s->plist_valid = plist0;
     s->step = step0;
     s->time = time0;
     s->cur = cur0;
@@ -608,6 +668,10 @@ int lqt_sim_step(lqt_sim *s, int64_t nsteps)
                 if (rc) return rc;
             }
             CK(cudaGraphLaunch(s->graph, s->stream));
+            if (s->sur) {
+                s->sur_launches += kGraphChunk / kSurSteps;   // chunks start on macro-step boundaries
+                s->plist_valid = true;
+            }
             s->step += kGraphChunk;
             for (int i = 0; i < kGraphChunk; ++i) s->time += s->p.dt;
             left -= kGraphChunk;
@@ -696,6 +760,10 @@ int lqt_sim_set_state(lqt_sim *s, const double *state_host)
     cudaFree(vtmp);
     s->mem.ptrs.erase(std::remove(s->mem.ptrs.begin(), s->mem.ptrs.end(), vtmp), s->mem.ptrs.end());
     if (e != cudaSuccess) return fail(LQT_ERR_CUDA, std::string("lqt_sim_set_state: ") + cudaGetErrorString(e));
+    // a new state ends any macro step in progress: every voxel runs the plain
+    // step until the next macro-step boundary
+    if (s->srate) CK(cudaMemset(s->srate, 0xff, s->ntissue * 4));
+    s->plist_valid = false;
     if (s->has_protocol) return refresh_windows(s, std::max<int64_t>(s->win_horizon, s->step + 1000));
     Clock c{};
     c.step = s->step;
@@ -797,27 +865,31 @@ int lqt_sim_tune(lqt_sim *s, int32_t variant, int32_t *chosen, float *ms_per_var
     return LQT_OK;
 }
 
-int lqt_sim_profile(lqt_sim *s, int64_t nsteps, double *ms_step, double *ms_ghost)
+int lqt_sim_profile(lqt_sim *s, int64_t nsteps, double *ms_step, double *ms_ghost, double *ms_sur)
 {
     if (!s || nsteps <= 0) return fail(LQT_ERR_INVALID, "lqt_sim_profile: NULL handle or nsteps <= 0");
-    cudaEvent_t ev[3];
+    cudaEvent_t ev[5];
     for (auto &e : ev) CK(cudaEventCreate(&e));
-    double t_step = 0, t_ghost = 0;
-    const StepK k = make_stepk(s->p.dt);
+    double t_step = 0, t_ghost = 0, t_sur = 0;
+    int64_t n_sur = 0;
     int rc = LQT_OK;
     for (int64_t i = 0; i < nsteps && rc == LQT_OK; ++i) {
-        cudaError_t e = cudaEventRecord(ev[0], s->stream);
-        if (s->fp64()) {
-            const GridDev<double> g = devf<double>(s);
-            if (e == cudaSuccess) e = launch_grid_step<double>(g, k, s->cur, s->dim, s->minb, s->stream);
-            if (e == cudaSuccess) e = cudaEventRecord(ev[1], s->stream);
-            if (e == cudaSuccess) e = launch_ghost<double>(g, s->cur ^ 1, s->stream);
-        } else {
-            const GridDev<float> g = devf<float>(s);
-            if (e == cudaSuccess) e = launch_grid_step<float>(g, k, s->cur, s->dim, s->minb, s->stream);
-            if (e == cudaSuccess) e = cudaEventRecord(ev[1], s->stream);
-            if (e == cudaSuccess) e = launch_ghost<float>(g, s->cur ^ 1, s->stream);
+        if (s->sur && s->step % kSurSteps == 0) {
+            cudaError_t e = cudaEventRecord(ev[3], s->stream);
+            if (e == cudaSuccess) rc = launch_sur_if_due(s);
+            if (e == cudaSuccess && rc == LQT_OK) e = cudaEventRecord(ev[4], s->stream);
+            if (e == cudaSuccess && rc == LQT_OK) e = cudaEventSynchronize(ev[4]);
+            float ms = 0;
+            if (e == cudaSuccess && rc == LQT_OK) e = cudaEventElapsedTime(&ms, ev[3], ev[4]);
+            if (e != cudaSuccess) rc = fail(LQT_ERR_CUDA, std::string("lqt_sim_profile: ") + cudaGetErrorString(e));
+            if (rc) break;
+            t_sur += ms;
+            ++n_sur;
         }
+        cudaError_t e = cudaEventRecord(ev[0], s->stream);
+        if (e == cudaSuccess) e = launch_substep(s);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[1], s->stream);
+        if (e == cudaSuccess) e = launch_ghost_now(s);
         if (e == cudaSuccess) e = cudaEventRecord(ev[2], s->stream);
         if (e == cudaSuccess) e = cudaEventSynchronize(ev[2]);
         float a = 0, b = 0;
@@ -834,6 +906,7 @@ int lqt_sim_profile(lqt_sim *s, int64_t nsteps, double *ms_step, double *ms_ghos
     if (rc) return rc;
     if (ms_step) *ms_step = t_step / nsteps;
     if (ms_ghost) *ms_ghost = t_ghost / nsteps;
+    if (ms_sur) *ms_sur = n_sur ? t_sur / n_sur : 0.0;
     return LQT_OK;
 }
 
@@ -854,6 +927,65 @@ int lqt_sim_check(lqt_sim *s, int64_t *n_bad)
     CK(cudaMemset(s->nbad, 0, sizeof(v)));
     *n_bad = (int64_t)v;
     return v ? LQT_ERR_NUMERIC : LQT_OK;
+}
+
+int lqt_sim_set_surrogate(lqt_sim *s, lqt_mlp *m, const lqt_sur_config *cfg)
+{
+    if (!s) return fail(LQT_ERR_INVALID, "lqt_sim_set_surrogate: NULL handle");
+    if (!m) {
+        s->sur = nullptr;
+        s->plist_valid = false;
+        s->graph_valid = false;
+        return LQT_OK;
+    }
+    if (s->fp64()) return fail(LQT_ERR_INVALID, "lqt_sim_set_surrogate: the surrogate runs in the mixed form only");
+    if (!cfg || !(cfg->dvdt_max > 0) || !(cfg->kappa > 0) || !(cfg->vstep_max > 0) || cfg->reserved != 0 ||
+        (cfg->use_net != 0 && cfg->use_net != 1))
+        return fail(LQT_ERR_INVALID, "lqt_sim_set_surrogate: dvdt_max, kappa, vstep_max > 0; use_net 0/1; reserved 0");
+    MlpDev w;
+    const float *nrm = nullptr;
+    if (!mlp_device_view(m, &w, &nrm)) return fail(LQT_ERR_INVALID, "lqt_sim_set_surrogate: network not initialised");
+    if (!s->srate) {
+        int rc = s->mem.alloc((void **)&s->srate, s->ntissue * 4) |
+                 s->mem.alloc((void **)&s->plist, s->ntissue * 4) |
+                 s->mem.alloc((void **)&s->plist_n, sizeof(unsigned long long)) |
+                 s->mem.alloc((void **)&s->sur_stats, 2 * sizeof(unsigned long long)) |
+                 s->mem.alloc((void **)&s->sur_err, sizeof(int));
+        if (rc) return LQT_ERR_NOMEM;
+        CK(cudaMemsetAsync(s->sur_stats, 0, 2 * sizeof(unsigned long long), s->stream));
+        CK(cudaMemsetAsync(s->sur_err, 0, sizeof(int), s->stream));
+    }
+    // NaN everywhere: plain steps until the first macro-step boundary
+    CK(cudaMemsetAsync(s->srate, 0xff, s->ntissue * 4, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    s->sur = m;
+    s->sur_cfg = *cfg;
+    s->plist_valid = false;
+    s->graph_valid = false;
+    return LQT_OK;
+}
+
+int lqt_sim_surrogate_stats(lqt_sim *s, int64_t *macro_steps, int64_t *offered, int64_t *accepted,
+                            int32_t *wait_timeouts, int32_t reset)
+{
+    if (!s) return fail(LQT_ERR_INVALID, "lqt_sim_surrogate_stats: NULL handle");
+    unsigned long long st[2] = {0, 0};
+    int err = 0;
+    if (s->sur_stats) {
+        CK(cudaStreamSynchronize(s->stream));
+        CK(cudaMemcpy(st, s->sur_stats, sizeof(st), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(&err, s->sur_err, sizeof(int), cudaMemcpyDeviceToHost));
+    }
+    if (macro_steps) *macro_steps = s->sur_launches;
+    if (offered) *offered = (int64_t)st[0];
+    if (accepted) *accepted = (int64_t)st[1];
+    if (wait_timeouts) *wait_timeouts = err;
+    if (reset && s->sur_stats) {
+        CK(cudaMemset(s->sur_stats, 0, sizeof(st)));
+        CK(cudaMemset(s->sur_err, 0, sizeof(int)));
+        s->sur_launches = 0;
+    }
+    return LQT_OK;
 }
 
 int lqt_sim_checkpoint(lqt_sim *s, const char *path)

@@ -122,8 +122,13 @@ __device__ __forceinline__ void det_open_cycle(DetState &d, float v_old)
 }
 
 // Returns true when an event (activation or APD90) happened this step.
+// peak_max: tissue grids keep the overshoot at the maximum V since activation
+// (a wave collision can stall an upstroke for one step, where the single-cell
+// rule "first non-rising step" would flip between the stall and the true peak
+// on a perturbation of a few microvolts); single cells and strands keep the
+// SingleCell.cc rule (peak_max = false).
 __device__ __forceinline__ bool det_step(DetState &d, float v_old, float v_new, float dvdt, float time,
-                                         float act_thr, float &t_act, DetEvent &ev)
+                                         float act_thr, float &t_act, DetEvent &ev, bool peak_max = false)
 {
     bool evt = false;
     ev.t_act = -1.f;
@@ -149,6 +154,10 @@ __device__ __forceinline__ bool det_step(DetState &d, float v_old, float v_new, 
         }
         break;
     case kDetFall: {
+        if (peak_max && v_new > d.vpeak) {
+            d.vpeak = v_new;
+            break;
+        }
         const float amp = d.vpeak - d.vrest;
         const float thr90 = d.vpeak - 0.9f * amp;
         const float thr50 = d.vpeak - 0.5f * amp;

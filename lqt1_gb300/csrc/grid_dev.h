@@ -52,6 +52,12 @@ template <typename R> struct GridDev {
     float act_thr;
     R vmin_ok, vmax_ok;
     unsigned long long *nbad;
+    // learned surrogate (mixed form): per tissue voxel, the ionic dV/dt fixed
+    // for the current macro step, or NaN where the plain step runs; and the
+    // list of the voxels that run the plain step (plist_n entries); null = off
+    const float *srate;
+    const int32_t *plist;
+    const int64_t *plist_n;
 };
 
 // Occupancy variants of k_grid_step: minimum CTAs/SM of 256 threads.
@@ -63,6 +69,7 @@ cudaError_t launch_grid_step(const GridDev<R> &gd, const StepK &k, int cur, int 
 template <typename R>
 cudaError_t launch_grid_step_minb(const GridDev<R> &gd, const StepT<R> &k, int cur, int dim, int minb, cudaStream_t st);
 template <typename R> cudaError_t launch_ghost(const GridDev<R> &gd, int nxt, cudaStream_t st);
+cudaError_t launch_sur_substep(const GridDev<float> &gd, double dt, int cur, int dim, cudaStream_t st);
 template <typename R>
 cudaError_t launch_ecg(const GridDev<R> &gd, int cur, const float4 *el, int nel, double *partial, double *out,
                        double *t_out, int64_t *counter, int64_t cap, int dim, cudaStream_t st);

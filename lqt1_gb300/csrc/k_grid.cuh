@@ -71,22 +71,51 @@ __device__ __forceinline__ R grid_du(const GridDev<R> &gd, const R *__restrict__
     }
 }
 
-// MINB = minimum resident CTAs per SM the register allocation must allow
-// (occupancy variants picked at run time by the autotuner in api_sim.cu; they
-// differ only in register allocation, not in arithmetic).
-template <typename R, int DIM, int MINB>
-__global__ void __launch_bounds__(256, MINB) k_grid_step(GridDev<R> gd, StepT<R> kst, int cur)
+// AP detector update of voxel k (record d) for one step from vc to vn.
+template <typename R>
+__device__ __forceinline__ void grid_detect_rec(const GridDev<R> &gd, const Clock &ck, int64_t k, float4 d, float vc,
+                                                float vn, float dvdt)
 {
-    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (k >= gd.ntissue) return;
-    const Clock ck = *gd.clk;
-    const R *__restrict__ V = gd.vg[cur];
-    R *__restrict__ Vn = gd.vg[cur ^ 1];
-    const int64_t g = DIM == 1 ? k : (int64_t)gd.gidx[k];
-    const R vc = V[g];
-    const R du = grid_du<R, DIM>(gd, V, g, k, vc);
+    DetState ds;
+    ds.vrest = d.x;
+    ds.vpeak = d.y;
+    uint32_t bits = __float_as_uint(d.w);
+    ds.phase = bits & 7u;
+    ds.ead = (bits >> 3) & 1u;
+    ds.dvdt_max = 0.f;
+    float t_act = d.z;
+    bool dirty = false;
+    if (ck.opened) {
+        det_open_cycle(ds, vc);
+        dirty = true;
+    }
+    if (ds.phase != kDetIdle && ds.phase != kDetDone) {
+        DetEvent ev;
+        const uint8_t ph0 = ds.phase;
+        const float vp0 = ds.vpeak;
+        const uint8_t e0 = ds.ead;
+        if (det_step(ds, vc, vn, dvdt, ck.time_f, gd.act_thr, t_act, ev, true)) {
+            if (ev.t_90 >= 0.f) gd.apd90[k] = ev.apd90;
+        }
+        dirty |= ds.phase != ph0 || ds.vpeak != vp0 || ds.ead != e0;
+    }
+    if (dirty) {
+        const uint32_t nb = (bits >> 4) + (ck.opened ? 1u : 0u);
+        gd.det[k] = make_float4(ds.vrest, ds.vpeak, t_act, __uint_as_float((nb << 4) | (ds.ead << 3) | ds.phase));
+    }
+}
 
-    const uint8_t ctl = gd.ctl[k];
+template <typename R>
+__device__ __forceinline__ void grid_detect(const GridDev<R> &gd, const Clock &ck, int64_t k, float vc, float vn,
+                                            float dvdt)
+{
+    grid_detect_rec(gd, ck, k, gd.det[k], vc, vn, dvdt);
+}
+
+// Stimulus current of voxel k at the clock's step.
+template <typename R>
+__device__ __forceinline__ R grid_stim(const GridDev<R> &gd, const Clock &ck, uint8_t ctl, int64_t k)
+{
     R ist = 0;
     if (gd.onset) {
         // per-voxel onset within each cycle (GPU3D.cu:397-409)
@@ -96,6 +125,39 @@ __global__ void __launch_bounds__(256, MINB) k_grid_step(GridDev<R> gd, StepT<R>
         ist = gd.s1_strength;
     }
     if (ck.s2_on && (ctl & kCtlS2)) ist = gd.s2_strength;
+    return ist;
+}
+
+template <typename R> __device__ __forceinline__ void grid_count_bad(const GridDev<R> &gd, R vn)
+{
+    const bool bad = !(vn == vn) || vn < gd.vmin_ok || vn > gd.vmax_ok;
+    const unsigned m = __ballot_sync(__activemask(), bad);
+    if (m && (threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(gd.nbad, (unsigned long long)__popc(m));
+}
+
+// MINB = minimum resident CTAs per SM the register allocation must allow
+// (occupancy variants picked at run time by the autotuner in api_sim.cu; they
+// differ only in register allocation, not in arithmetic).  With the learned
+// surrogate attached, the launch covers only the voxels listed in plist (the
+// ones that run the plain step during the current macro step).
+template <typename R, int DIM, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_grid_step(GridDev<R> gd, StepT<R> kst, int cur)
+{
+    int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (gd.plist) {
+        if (k >= *gd.plist_n) return;
+        k = gd.plist[k];
+    } else if (k >= gd.ntissue) {
+        return;
+    }
+    const Clock ck = *gd.clk;
+    const R *__restrict__ V = gd.vg[cur];
+    R *__restrict__ Vn = gd.vg[cur ^ 1];
+    const int64_t g = DIM == 1 ? k : (int64_t)gd.gidx[k];
+    const R vc = V[g];
+    const R du = grid_du<R, DIM>(gd, V, g, k, vc);
+    const uint8_t ctl = gd.ctl[k];
+    const R ist = grid_stim(gd, ck, ctl, k);
 
     CellState<R> c;
     load_cell(c, gd.s, k);
@@ -104,41 +166,71 @@ __global__ void __launch_bounds__(256, MINB) k_grid_step(GridDev<R> gd, StepT<R>
     tpord_step<R>(c, ctl & kCtlType, gd.model, kst, ist, du, &o);
     store_cell(c, gd.s, k);
     Vn[g] = c.v;
+    if (gd.det) grid_detect(gd, ck, k, (float)vc, (float)c.v, (float)o.dvdt);
+    grid_count_bad(gd, c.v);
+}
 
-    if (gd.det) {
-        float4 d = gd.det[k];
-        DetState ds;
-        ds.vrest = d.x;
-        ds.vpeak = d.y;
-        uint32_t bits = __float_as_uint(d.w);
-        ds.phase = bits & 7u;
-        ds.ead = (bits >> 3) & 1u;
-        ds.dvdt_max = 0.f;
-        float t_act = d.z;
-        bool dirty = false;
-        if (ck.opened) {
-            det_open_cycle(ds, (float)vc);
-            dirty = true;
+// Inside a surrogate macro step: the voxels whose ionic change is fixed
+// (srate not NaN) move V by it plus diffusion, in the update form of
+// TPORd.cc:928-930; the others are left to k_grid_step over plist.  Every
+// per-voxel load that depends only on k (rate, grid index, control byte,
+// diffusion tensor, detector record) is issued before the first use, so a
+// voxel costs two memory round trips (those, then the V stencil).
+template <int DIM> __global__ void __launch_bounds__(256) k_sur_substep(GridDev<float> gd, float dt, int cur)
+{
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= gd.ntissue) return;
+    const float r = gd.srate[k];
+    const int64_t g = DIM == 1 ? k : (int64_t)gd.gidx[k];
+    const uint8_t ctl = gd.ctl[k];
+    float Dt[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, Bt[3] = {0.f, 0.f, 0.f};
+    const bool aniso = DIM > 1 && gd.d6;
+    if (aniso) {
+#pragma unroll
+        for (int i = 0; i < (DIM == 3 ? 6 : 4); ++i) Dt[i] = __ldg(gd.d6 + 6 * k + i);
+#pragma unroll
+        for (int i = 0; i < (DIM == 3 ? 3 : 2); ++i) Bt[i] = __ldg(gd.b3 + 3 * k + i);
+    }
+    float4 det = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (gd.det) det = gd.det[k];
+    if (!(r == r)) return;
+    const Clock ck = *gd.clk;
+    const float *__restrict__ V = gd.vg[cur];
+    float *__restrict__ Vn = gd.vg[cur ^ 1];
+    const float vc = V[g];
+    float du;
+    if (DIM == 1 || !aniso) {
+        du = grid_du<float, DIM>(gd, V, g, k, vc);
+    } else {
+        // the anisotropic stencil of grid_du with the tensor already loaded
+        const int64_t sx = gd.sx, sy = gd.sy;
+        const float vxp = V[g + sx], vxm = V[g - sx], vyp = V[g + sy], vym = V[g - sy];
+        const float lxy0 = V[g + sx + sy], lxy1 = V[g - sx - sy], lxy2 = V[g - sx + sy], lxy3 = V[g + sx - sy];
+        float vzp = 0.f, vzm = 0.f, z0 = 0.f, z1 = 0.f, z2 = 0.f, z3 = 0.f, y0 = 0.f, y1 = 0.f, y2 = 0.f, y3 = 0.f;
+        if constexpr (DIM == 3) {
+            vzp = V[g + 1];
+            vzm = V[g - 1];
+            z0 = V[g + sx + 1]; z1 = V[g - sx - 1]; z2 = V[g - sx + 1]; z3 = V[g + sx - 1];
+            y0 = V[g + sy + 1]; y1 = V[g - sy - 1]; y2 = V[g - sy + 1]; y3 = V[g + sy - 1];
         }
-        if (ds.phase != kDetIdle && ds.phase != kDetDone) {
-            DetEvent ev;
-            const uint8_t ph0 = ds.phase;
-            const float vp0 = ds.vpeak;
-            const uint8_t e0 = ds.ead;
-            if (det_step(ds, (float)vc, (float)c.v, (float)o.dvdt, ck.time_f, gd.act_thr, t_act, ev)) {
-                if (ev.t_90 >= 0.f) gd.apd90[k] = ev.apd90;
-            }
-            dirty |= ds.phase != ph0 || ds.vpeak != vp0 || ds.ead != e0;
-        }
-        if (dirty) {
-            const uint32_t nb = (bits >> 4) + (ck.opened ? 1u : 0u);
-            gd.det[k] = make_float4(ds.vrest, ds.vpeak, t_act, __uint_as_float((nb << 4) | (ds.ead << 3) | ds.phase));
+        const float c2 = gd.inv_dx2, c4 = gd.inv_4dx2, c1 = gd.inv_2dx;
+        const float lxx = (vxp + vxm - 2.f * vc) * c2;
+        const float lyy = (vyp + vym - 2.f * vc) * c2;
+        const float lxy = (lxy0 + lxy1 - lxy2 - lxy3) * c4;
+        du = Dt[0] * lxx + Dt[1] * lyy + 2.f * Dt[3] * lxy + Bt[0] * ((vxp - vxm) * c1) + Bt[1] * ((vyp - vym) * c1);
+        if constexpr (DIM == 3) {
+            const float lzz = (vzp + vzm - 2.f * vc) * c2;
+            const float lxz = (z0 + z1 - z2 - z3) * c4;
+            const float lyz = (y0 + y1 - y2 - y3) * c4;
+            du += Dt[2] * lzz + 2.f * (Dt[4] * lxz + Dt[5] * lyz) + Bt[2] * ((vzp - vzm) * c1);
         }
     }
-    const R vn = c.v;
-    const bool bad = !(vn == vn) || vn < gd.vmin_ok || vn > gd.vmax_ok;
-    const unsigned m = __ballot_sync(__activemask(), bad);
-    if (m && (threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(gd.nbad, (unsigned long long)__popc(m));
+    const float ist = grid_stim(gd, ck, ctl, k);
+    const float dvdt = r - ist;
+    const float vn = vc + (dvdt + du) * dt;
+    Vn[g] = vn;
+    if (gd.det) grid_detect_rec(gd, ck, k, det, vc, vn, dvdt);
+    grid_count_bad(gd, vn);
 }
 
 // Mirror-boundary refresh of the new grid, then the clock advance for the

@@ -2,8 +2,8 @@
 //   * training pairs generated by the plain mixed-form TPORd step,
 //   * feature normalisation into the network's BF16 inputs.
 // A surrogate macro step advances a cell by kSurSteps plain steps (0.1 ms at
-// dt = 0.02 ms) with no diffusion and no stimulus: the network predicts the
-// change of the 38 evolving states.
+// dt = 0.02 ms) with no diffusion and no stimulus: one coarse TPORd step of
+// 0.1 ms plus the network's correction of the 38 evolving states.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -11,92 +11,76 @@
 #include "common.cuh"
 #include "mlp.h"
 #include "sur.h"
+#include "sur_dev.cuh"
 
 namespace lqt {
 
-// The 38 evolving states in network order: V, 8 concentrations, 29 gates.
-template <typename R> __device__ __forceinline__ void state38(const CellState<R> &c, float *x)
+__device__ __forceinline__ void sur_init_cell(CellState<float> &c)
 {
-    x[0] = (float)c.v;
-    const typename CellState<R>::C *cc[8] = {&c.nai, &c.nass, &c.ki, &c.kss, &c.cai, &c.cass, &c.cansr, &c.cajsr};
-#pragma unroll
-    for (int j = 0; j < 8; ++j) x[1 + j] = (float)cval(*cc[j]);
-    const R g[29] = {c.sm, c.sh, c.sj, c.mL, c.hL, c.hLp, c.a, c.iF, c.iS, c.ap, c.iFp, c.iSp, c.d, c.ff, c.fs,
-                     c.fcaf, c.fcas, c.jca, c.nca, c.ffp, c.fcafp, c.xrf, c.xrs, c.xs1, c.xs2, c.xk1, c.Jrelnp,
-                     c.Jrelp, c.CaMKt};
-#pragma unroll
-    for (int j = 0; j < 29; ++j) x[9 + j] = (float)g[j];
-}
-
-__device__ __forceinline__ uint32_t hash3(uint64_t s, uint64_t a, uint64_t b)
-{
-    uint64_t x = s ^ (a * 0x9E3779B97F4A7C15ull) ^ (b * 0xC2B2AE3D27D4EB4Full);
-    x ^= x >> 33;
-    x *= 0xFF51AFD7ED558CCDull;
-    x ^= x >> 33;
-    x *= 0xC4CEB9FE1A85EC53ull;
-    x ^= x >> 33;
-    return (uint32_t)x;
+    c.v = -87.5f;
+    c.nai = make_float2(7.f, 0.f); c.nass = make_float2(7.f, 0.f);
+    c.ki = make_float2(145.f, 0.f); c.kss = make_float2(145.f, 0.f);
+    c.cai = make_float2(1.0e-4f, 0.f); c.cass = make_float2(1.0e-4f, 0.f);
+    c.cansr = make_float2(1.2f, 0.f); c.cajsr = make_float2(1.2f, 0.f);
+    c.sm = 0.f; c.sh = 1.f; c.sj = 1.f; c.mL = 0.f; c.hL = 1.f; c.hLp = 1.f; c.a = 0.f; c.iF = 1.f; c.iS = 1.f;
+    c.ap = 0.f; c.iFp = 1.f; c.iSp = 1.f; c.d = 0.f; c.ff = 1.f; c.fs = 1.f; c.fcaf = 1.f; c.fcas = 1.f;
+    c.jca = 1.f; c.nca = 0.f; c.ffp = 1.f; c.fcafp = 1.f; c.xrf = 0.f; c.xrs = 0.f; c.xs1 = 0.f; c.xs2 = 0.f;
+    c.xk1 = 1.f; c.Jrelnp = 0.f; c.Jrelp = 0.f; c.CaMKt = 0.f;
 }
 
 // One thread per cell: pace with the plain mixed step, and at macro-step
 // boundaries in the surrogate's regime (|dV/dt| <= dvdt_max, no stimulus in
 // the coming macro step, past the warm-up) record, with probability `prob`,
-// the inputs and the state change over the macro step.
+// the inputs and the correction: state after kSurSteps plain steps minus the
+// state after one coarse step of the macro length from the same start.
+// Macro steps that are not recorded carry a constant current uniform in
+// +-jitter (a stand-in for the electrotonic load of tissue).
 __global__ void __launch_bounds__(128) k_sur_datagen(const SurCell *__restrict__ cells, int64_t ncells,
                                                      const ModelK *__restrict__ models, StepT<float> k,
-                                                     float *__restrict__ X, float *__restrict__ D,
-                                                     unsigned long long *__restrict__ counter, int64_t cap,
-                                                     uint64_t seed, float dvdt_max, float prob)
+                                                     StepT<float> kmac, float *__restrict__ X,
+                                                     float *__restrict__ D, unsigned long long *__restrict__ counter,
+                                                     int64_t cap, uint64_t seed, float dvdt_max, float prob,
+                                                     float jitter)
 {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= ncells) return;
     const SurCell sc = cells[i];
     const ModelT<float> m = model_as<float>(models[sc.model]);
     CellState<float> c;
-    c.v = -87.5f;
-    const float2 z = make_float2(0.f, 0.f);
-    c.nai = make_float2(7.f, 0.f); c.nass = make_float2(7.f, 0.f);
-    c.ki = make_float2(145.f, 0.f); c.kss = make_float2(145.f, 0.f);
-    c.cai = make_float2(1.0e-4f, 0.f); c.cass = make_float2(1.0e-4f, 0.f);
-    c.cansr = make_float2(1.2f, 0.f); c.cajsr = make_float2(1.2f, 0.f);
-    (void)z;
-    c.sm = 0.f; c.sh = 1.f; c.sj = 1.f; c.mL = 0.f; c.hL = 1.f; c.hLp = 1.f; c.a = 0.f; c.iF = 1.f; c.iS = 1.f;
-    c.ap = 0.f; c.iFp = 1.f; c.iSp = 1.f; c.d = 0.f; c.ff = 1.f; c.fs = 1.f; c.fcaf = 1.f; c.fcas = 1.f;
-    c.jca = 1.f; c.nca = 0.f; c.ffp = 1.f; c.fcafp = 1.f; c.xrf = 0.f; c.xrs = 0.f; c.xs1 = 0.f; c.xs2 = 0.f;
-    c.xk1 = 1.f; c.Jrelnp = 0.f; c.Jrelp = 0.f; c.CaMKt = 0.f;
+    sur_init_cell(c);
     const int ct = sc.ctype;
-    const int cls = ct == 2 ? 1 : (ct == 4 ? 2 : 0);
+    const int cls = sur_class(ct);
     StepOut<float> o{};
     int64_t slot = -1;
-    float x0[kMlpNState];
-    float lo0[8];
+    float xc[kMlpNState];   // coarse end state (hi parts) of the pending sample
+    float loc[8];           // and its concentration lo parts
+    float ipert = 0.f;
     for (int64_t st = 0; st < sc.nsteps; ++st) {
         const int64_t ph = st % sc.bcl_steps;
         if (st % kSurSteps == 0) {
             if (slot >= 0) {
-                // finish the pending sample: change over the macro step
+                // finish the pending sample: fine minus coarse
                 float x1[kMlpNState];
                 state38(c, x1);
+                float2 *cp[8];
+                conc_ptrs(c, cp);
                 float *d = D + slot * kMlpNState;
-                const float2 *cc[8] = {&c.nai, &c.nass, &c.ki, &c.kss, &c.cai, &c.cass, &c.cansr, &c.cajsr};
-                d[0] = x1[0] - x0[0];
+                d[0] = x1[0] - xc[0];
 #pragma unroll
-                for (int j = 0; j < 8; ++j) d[1 + j] = (cc[j]->x - x0[1 + j]) + (cc[j]->y - lo0[j]);
+                for (int j = 0; j < 8; ++j) d[1 + j] = (cp[j]->x - xc[1 + j]) + (cp[j]->y - loc[j]);
 #pragma unroll
-                for (int j = 9; j < kMlpNState; ++j) d[j] = x1[j] - x0[j];
+                for (int j = 9; j < kMlpNState; ++j) d[j] = x1[j] - xc[j];
                 slot = -1;
             }
             const bool stim_ahead = ph + kSurSteps > sc.stim_on && ph < sc.stim_off;
+            ipert = 0.f;
             if (st >= sc.warm_steps && !stim_ahead && fabsf(o.dvdt) <= dvdt_max && st + kSurSteps <= sc.nsteps &&
-                (hash3(seed, (uint64_t)i, (uint64_t)st) & 0xFFFFFF) < (uint32_t)(prob * 16777216.f)) {
+                (sur_hash(seed, (uint64_t)i, (uint64_t)st) & 0xFFFFFF) < (uint32_t)(prob * 16777216.f)) {
                 const unsigned long long s = atomicAdd(counter, 1ull);
                 if (s < (unsigned long long)cap) {
                     slot = (int64_t)s;
+                    float x0[kMlpNState];
                     state38(c, x0);
-                    const float2 *cc[8] = {&c.nai, &c.nass, &c.ki, &c.kss, &c.cai, &c.cass, &c.cansr, &c.cajsr};
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) lo0[j] = cc[j]->y;
                     float *xr = X + slot * kSurFeat;
 #pragma unroll
                     for (int j = 0; j < kMlpNState; ++j) xr[j] = x0[j];
@@ -106,10 +90,21 @@ __global__ void __launch_bounds__(128) k_sur_datagen(const SurCell *__restrict__
                     xr[41] = cls == 0;
                     xr[42] = cls == 1;
                     xr[43] = cls == 2;
+                    CellState<float> cc = c;
+                    StepOut<float> oc;
+                    tpord_step<float>(cc, ct, m, kmac, 0.f, 0.f, &oc);
+                    state38(cc, xc);
+                    float2 *cp[8];
+                    conc_ptrs(cc, cp);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) loc[j] = cp[j]->y;
                 }
+            } else if (jitter > 0.f && !stim_ahead) {
+                const uint32_t h = sur_hash(seed ^ 0x5bd1e995ull, (uint64_t)i, (uint64_t)st);
+                ipert = jitter * ((float)(h >> 8) * (2.0f / 16777216.0f) - 1.0f);
             }
         }
-        const float ist = (ph >= sc.stim_on && ph < sc.stim_off) ? sc.stim : 0.f;
+        const float ist = (ph >= sc.stim_on && ph < sc.stim_off) ? sc.stim : (slot >= 0 ? 0.f : ipert);
         tpord_step<float>(c, ct, m, k, ist, 0.f, &o);
     }
 }
@@ -134,13 +129,14 @@ __global__ void k_sur_prepare(const float *__restrict__ X, const float *__restri
     }
 }
 
-cudaError_t launch_sur_datagen(const SurCell *cells, int64_t ncells, const ModelK *models, const StepK &k, float *X,
-                               float *D, unsigned long long *counter, int64_t cap, uint64_t seed, float dvdt_max,
-                               float prob, cudaStream_t st)
+cudaError_t launch_sur_datagen(const SurCell *cells, int64_t ncells, const ModelK *models, const StepK &k,
+                               const StepK &kmac, float *X, float *D, unsigned long long *counter, int64_t cap,
+                               uint64_t seed, float dvdt_max, float prob, float jitter, cudaStream_t st)
 {
     if (ncells <= 0) return cudaSuccess;
-    k_sur_datagen<<<(unsigned)((ncells + 127) / 128), 128, 0, st>>>(cells, ncells, models, step_as<float>(k), X, D,
-                                                                    counter, cap, seed, dvdt_max, prob);
+    k_sur_datagen<<<(unsigned)((ncells + 127) / 128), 128, 0, st>>>(cells, ncells, models, step_as<float>(k),
+                                                                    step_as<float>(kmac), X, D, counter, cap, seed,
+                                                                    dvdt_max, prob, jitter);
     return cudaGetLastError();
 }
 

@@ -21,6 +21,12 @@ struct MlpDev {
     const float *b1, *b2, *b3;              // [128], [128], [48]
 };
 
+}  // namespace lqt
+struct lqt_mlp;
+namespace lqt {
+// Device weights and normalisation (in_mean, in_scale, out_scale) of a network.
+bool mlp_device_view(const lqt_mlp *m, MlpDev *w, const float **norm);
+
 cudaError_t launch_mlp_infer_tc(const __nv_bfloat16 *X, float *Y, const MlpDev &w, int64_t n, int *err, int swap,
                                 cudaStream_t st);
 

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "grid_dev.h"
+#include "mlp.h"
 #include "tpord.cuh"
 
 namespace lqt {
@@ -20,9 +22,29 @@ struct SurCell {
     float gks_scale, pca_scale, iso_scale;
 };
 
-cudaError_t launch_sur_datagen(const SurCell *cells, int64_t ncells, const ModelK *models, const StepK &k, float *X,
-                               float *D, unsigned long long *counter, int64_t cap, uint64_t seed, float dvdt_max,
-                               float prob, cudaStream_t st);
+// The tissue macro step (k_sur_grid.cu).
+struct SurGrid {
+    MlpDev w;
+    const float *norm;              // in_mean[48], in_scale[48], out_scale[48], out_bound[48]
+    float *rate;                    // per tissue voxel: ionic dV/dt of the macro step, NaN = plain step
+    int32_t *plist;                 // voxels that run the plain step during the macro step
+    unsigned long long *plist_n;    // their count (zero before the launch)
+    unsigned long long *stats;      // [0] voxels offered, [1] accepted
+    int *err;                       // set when an mbarrier wait ran out
+    StepT<float> kmac;              // the coarse step (dt = nsub * plain dt)
+    float par[3];                   // GKs, PCa and GKs-ISO factors of the model
+    float dvdt_max;                 // offer only where |dV/dt| <= dvdt_max (mV/ms)
+    float kappa;                    // multiplier of out_bound in the residual check
+    float vstep_max;                // bound on the macro step's ionic V change (mV)
+    int nsub;                       // plain steps per macro step
+    int use_net;                    // 0: coarse step without the network
+};
+cudaError_t launch_sur_grid(const GridDev<float> &gd, const SurGrid &sg, int cur, int dim, cudaStream_t st);
+uint32_t sur_grid_smem_bytes();
+
+cudaError_t launch_sur_datagen(const SurCell *cells, int64_t ncells, const ModelK *models, const StepK &k,
+                               const StepK &kmac, float *X, float *D, unsigned long long *counter, int64_t cap,
+                               uint64_t seed, float dvdt_max, float prob, float jitter, cudaStream_t st);
 cudaError_t launch_sur_prepare(const float *X, const float *D, const int64_t *idx, int64_t n, const float *norm,
                                __nv_bfloat16 *xb, float *t, cudaStream_t st);
 

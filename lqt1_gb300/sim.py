@@ -112,13 +112,40 @@ class Sim:
         return ch.value, ms
 
     def profile(self, nsteps: int = 20):
-        """Mean device ms per launch of the fused step kernel and of the ghost
-        kernel (CUDA events on the simulation's stream)."""
+        """Mean device ms per launch of the fused step kernel, of the ghost
+        kernel and (with a surrogate attached) of the surrogate macro-step
+        kernel, 0 when none ran (CUDA events on the simulation's stream)."""
         L = N.lib()
-        L.lqt_sim_profile.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double)]
-        a, b = C.c_double(), C.c_double()
-        N.check(L.lqt_sim_profile(self._h, int(nsteps), C.byref(a), C.byref(b)), "lqt_sim_profile")
-        return a.value, b.value
+        L.lqt_sim_profile.argtypes = [C.c_void_p, C.c_int64] + [C.POINTER(C.c_double)] * 3
+        a, b, c = C.c_double(), C.c_double(), C.c_double()
+        N.check(L.lqt_sim_profile(self._h, int(nsteps), C.byref(a), C.byref(b), C.byref(c)), "lqt_sim_profile")
+        return a.value, b.value, c.value
+
+    # ---- learned surrogate ---------------------------------------------------------
+    def set_surrogate(self, mlp=None, *, dvdt_max: float = 1.0, kappa: float = 1.5, vstep_max: float = 0.3,
+                      use_net: bool = True):
+        """Attach a trained surrogate network (lqt1_gb300.surrogate.Mlp) or
+        detach (None).  Mixed form only; see lqt_sim_set_surrogate."""
+        L = N.lib()
+        L.lqt_sim_set_surrogate.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        if mlp is None:
+            N.check(L.lqt_sim_set_surrogate(self._h, None, None), "lqt_sim_set_surrogate")
+            self._sur = None
+            return
+        cfg = N.SurConfig(dvdt_max, kappa, vstep_max, int(bool(use_net)), 0)
+        N.check(L.lqt_sim_set_surrogate(self._h, mlp._h, C.byref(cfg)), "lqt_sim_set_surrogate")
+        self._sur = mlp     # keep the network alive while attached
+
+    def surrogate_stats(self, reset: bool = False):
+        """Macro steps launched, voxel offers, voxels accepted, wait timeouts."""
+        L = N.lib()
+        L.lqt_sim_surrogate_stats.argtypes = [C.c_void_p] + [C.POINTER(C.c_int64)] * 3 + [C.POINTER(C.c_int32),
+                                                                                             C.c_int32]
+        m, o, a = C.c_int64(), C.c_int64(), C.c_int64()
+        t = C.c_int32()
+        N.check(L.lqt_sim_surrogate_stats(self._h, C.byref(m), C.byref(o), C.byref(a), C.byref(t), int(reset)),
+                "lqt_sim_surrogate_stats")
+        return dict(macro_steps=m.value, offered=o.value, accepted=a.value, wait_timeouts=t.value)
 
     def boundary(self):
         L = N.lib()

@@ -8,6 +8,8 @@ owned by the caller.
 from __future__ import annotations
 
 import ctypes as C
+import json
+import os
 
 import numpy as np
 
@@ -27,6 +29,7 @@ def _bind():
         "lqt_mlp_set_params": ([P, P], C.c_int),
         "lqt_mlp_get_params": ([P, P, P], C.c_int),
         "lqt_mlp_set_norm": ([P, P, P, P, C.c_int32], C.c_int),
+        "lqt_mlp_set_bounds": ([P, P], C.c_int),
         "lqt_mlp_set_layout": ([P, C.c_int32], C.c_int),
         "lqt_mlp_infer": ([P, P, P, C.c_int64], C.c_int),
         "lqt_mlp_gradients": ([P, P, P, C.c_int64, C.POINTER(C.c_double)], C.c_int),
@@ -73,6 +76,12 @@ class Mlp:
         N.check(self.L.lqt_mlp_set_norm(self._h, a[0].ctypes.data, a[1].ctypes.data, a[2].ctypes.data, nvalid),
                 "lqt_mlp_set_norm")
 
+    def set_bounds(self, out_bound):
+        """Residual bounds (normalised units) for the tissue macro step."""
+        b = np.ascontiguousarray(out_bound, np.float32)
+        self.out_bound = b
+        N.check(self.L.lqt_mlp_set_bounds(self._h, b.ctypes.data), "lqt_mlp_set_bounds")
+
     def set_layout(self, layout: int):
         N.check(self.L.lqt_mlp_set_layout(self._h, layout), "lqt_mlp_set_layout")
 
@@ -96,7 +105,7 @@ class Mlp:
 class SurRanges(C.Structure):
     _fields_ = [("gks", C.c_double * 2), ("pca", C.c_double * 2), ("iso", C.c_double * 2), ("bcl", C.c_double * 2),
                 ("beats_warm", C.c_int32), ("beats_record", C.c_int32), ("dt", C.c_double), ("dvdt_max", C.c_double),
-                ("prob", C.c_double)]
+                ("prob", C.c_double), ("jitter", C.c_double)]
 
 
 def _bind_sur():
@@ -111,19 +120,34 @@ def _bind_sur():
 
 
 def generate(ncells=65536, seed=1, cap=20_000_000, *, gks=(0.05, 1.0), pca=(1.0, 2.2), iso=(1.0, 2.0),
-             bcl=(400.0, 2000.0), beats_warm=3, beats_record=6, dvdt_max=2.0, prob=0.05, dt=0.02, stream=None):
+             bcl=(400.0, 2000.0), beats_warm=0, beats_record=6, dvdt_max=2.0, prob=0.005, jitter=0.3, dt=0.02,
+             stream=None):
     """Training pairs from the plain mixed-form integrator on the GPU.
-    Returns torch tensors X [n, 44] (raw features) and D [n, 38] (changes over 0.1 ms)."""
+    Returns torch tensors X [n, 44] (raw features) and D [n, 38] (fine minus
+    coarse state after 0.1 ms)."""
     import torch
     L = _bind_sur()
     X = torch.empty((cap, 44), dtype=torch.float32, device="cuda")
     D = torch.empty((cap, N_STATE), dtype=torch.float32, device="cuda")
     r = SurRanges((C.c_double * 2)(*gks), (C.c_double * 2)(*pca), (C.c_double * 2)(*iso), (C.c_double * 2)(*bcl),
-                  beats_warm, beats_record, dt, dvdt_max, prob)
+                  beats_warm, beats_record, dt, dvdt_max, prob, jitter)
     n = C.c_int64()
     N.check(L.lqt_sur_datagen(ncells, seed, C.byref(r), X.data_ptr(), D.data_ptr(), cap, C.byref(n),
                               C.c_void_p(stream or 0)), "lqt_sur_datagen")
     return X[:n.value], D[:n.value]
+
+
+def fit_bounds(D, out_scale):
+    """Largest |normalised target| of each output over the whole set (the
+    residual bounds); outputs without a target get 1."""
+    import torch
+    osc = torch.from_numpy(np.ascontiguousarray(out_scale[:N_STATE], np.float32)).cuda()
+    mx = torch.zeros(N_STATE, device="cuda")
+    for i in range(0, D.shape[0], 1 << 22):
+        mx = torch.maximum(mx, (D[i:i + (1 << 22)].abs() / osc).amax(0))
+    b = np.ones(OUT, np.float32)
+    b[:N_STATE] = np.maximum(mx.cpu().numpy(), 1e-3)
+    return b
 
 
 def fit_norm(X, D, nsample=500_000, seed=0):
@@ -180,8 +204,8 @@ def train(mlp: Mlp, X, D, *, epochs=4, batch=8192, lr=2e-3, lr_min=1e-4, holdout
 
 
 def validate(mlp: Mlp, Xv, Dv, out_scale=None):
-    """Per-state RMSE of the predicted change over 0.1 ms (physical units) and
-    the RMSE of the zero-change baseline, on tcgen05 inference."""
+    """Per-state RMSE of the predicted correction (physical units) and the
+    RMSE of the zero correction (the coarse step alone), on tcgen05 inference."""
     import torch
     L = _bind_sur()
     n = Xv.shape[0]
@@ -195,3 +219,83 @@ def validate(mlp: Mlp, Xv, Dv, out_scale=None):
     rmse = np.sqrt(((pred - true) ** 2).mean(0))
     base = np.sqrt((true ** 2).mean(0))
     return dict(rmse=rmse, zero_rmse=base, n=n)
+
+
+DEFAULT_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "tpord_surrogate.npz")
+
+
+def save(mlp: Mlp, path: str, meta: dict | None = None):
+    os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
+    np.savez(path, params=mlp.params(), in_mean=mlp.norm_in_mean, in_scale=mlp.norm_in_scale,
+             out_scale=mlp.norm_out, out_bound=getattr(mlp, "out_bound", np.full(OUT, np.inf, np.float32)),
+             meta=np.array(json.dumps(meta or {})))
+
+
+def load(path: str | None = None, stream: int | None = None) -> Mlp:
+    """A network with the weights and normalisation of a saved file (the
+    shipped TPORd surrogate by default)."""
+    z = np.load(path or DEFAULT_WEIGHTS)
+    m = Mlp(seed=0, stream=stream)
+    m.set_params(z["params"])
+    m.set_norm(z["in_mean"], z["in_scale"], z["out_scale"])
+    if "out_bound" in z.files and np.isfinite(z["out_bound"]).all():
+        m.set_bounds(z["out_bound"])
+    m.meta = json.loads(str(z["meta"]))
+    return m
+
+
+def train_default(out=DEFAULT_WEIGHTS, *, ncells=65536, cap=20_000_000, prob=0.005, epochs=12, batch=8192,
+                  lr=2e-3, seed=1, log=print):
+    """Generate the pairs, fit the normalisation, train, validate, save."""
+    import time
+
+    import torch
+    t0 = time.perf_counter()
+    X, D = generate(ncells=ncells, cap=cap, prob=prob, seed=seed)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    log(f"pairs {X.shape[0]} in {t1 - t0:.1f} s")
+    m = Mlp(seed=seed)
+    im, isc, osc = fit_norm(X, D)
+    m.set_norm(im, isc, osc)
+    m.set_bounds(fit_bounds(D, osc))
+    val, hist = train(m, X, D, epochs=epochs, batch=batch, lr=lr, seed=seed, log=log)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    rel = val["rmse"] / np.maximum(val["zero_rmse"], 1e-30)
+    meta = dict(pairs=int(X.shape[0]), ncells=ncells, epochs=epochs, batch=batch, lr=lr, seed=seed, dt=0.02,
+                macro_steps=5, gen_s=t1 - t0, train_s=t2 - t1, loss_history=[(int(k), float(l)) for k, l in hist],
+                val_rmse=val["rmse"].tolist(), val_zero_rmse=val["zero_rmse"].tolist(), val_n=int(val["n"]),
+                state_names=STATE_NAMES)
+    save(m, out, meta)
+    log(json.dumps({"pairs": meta["pairs"], "gen_s": round(meta["gen_s"], 2), "train_s": round(meta["train_s"], 2),
+                    "final_loss": hist[-1][1] if hist else None,
+                    "rmse_over_coarse_median": float(np.median(rel)), "rmse_over_coarse_max": float(rel.max()),
+                    "v_rmse_mV": float(val["rmse"][0]), "v_coarse_rmse_mV": float(val["zero_rmse"][0])}))
+    return m, meta
+
+
+STATE_NAMES = ["v", "nai", "nass", "ki", "kss", "cai", "cass", "cansr", "cajsr", "m", "h", "j", "mL", "hL", "hLp",
+               "a", "iF", "iS", "ap", "iFp", "iSp", "d", "ff", "fs", "fcaf", "fcas", "jca", "nca", "ffp", "fcafp",
+               "xrf", "xrs", "xs1", "xs2", "xk1", "Jrelnp", "Jrelp", "CaMKt"]
+
+
+def main():
+    import argparse
+    ap = argparse.ArgumentParser(description="Train the TPORd surrogate on the GPU")
+    ap.add_argument("what", choices=["train"])
+    ap.add_argument("--out", default=DEFAULT_WEIGHTS)
+    ap.add_argument("--cells", type=int, default=65536)
+    ap.add_argument("--pairs", type=int, default=20_000_000)
+    ap.add_argument("--prob", type=float, default=0.005)
+    ap.add_argument("--epochs", type=int, default=12)
+    ap.add_argument("--batch", type=int, default=8192)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--seed", type=int, default=1)
+    a = ap.parse_args()
+    train_default(a.out, ncells=a.cells, cap=a.pairs, prob=a.prob, epochs=a.epochs, batch=a.batch, lr=a.lr,
+                  seed=a.seed, log=lambda m: print(m, flush=True))
+
+
+if __name__ == "__main__":
+    main()

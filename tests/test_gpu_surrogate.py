@@ -1,0 +1,201 @@
+"""The learned surrogate on the GPU: its training pairs against the FP64 oracle,
+the fused tissue macro step against the network's own inference kernel, its
+accuracy against the FP64 form, and what the trained network gains over the
+coarse step alone (accuracy) and over plain stepping (speed)."""
+import os
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+# network order of the 38 evolving states -> reference state index (0..39):
+# V, 8 concentrations, then gate slots 0..30 without hsp/jp (slots 3, 4)
+REF_INDEX = [0] + list(range(1, 9)) + [9 + (j if j < 3 else j + 2) for j in range(29)]
+
+
+@pytest.fixture(scope="module")
+def lq():
+    import lqt1_gb300 as lq
+    lq.lib()
+    return lq
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def net(lq):
+    from lqt1_gb300 import surrogate as S
+    if not os.path.exists(S.DEFAULT_WEIGHTS):
+        pytest.fail("trained surrogate weights missing: " + S.DEFAULT_WEIGHTS)
+    return S.load()
+
+
+def test_datagen_pairs_match_oracle(lq, orc, torch):
+    """Each training pair = (state, 5 plain steps of 0.02 ms minus one coarse
+    step of 0.1 ms from that state); recomputed by the FP64 oracle from the
+    recorded FP32 state."""
+    from lqt1_gb300 import surrogate as S
+    X, D = S.generate(ncells=256, cap=4000, prob=0.02, beats_warm=0, beats_record=2, bcl=(400.0, 600.0), seed=5,
+                      jitter=0.3)
+    X, D = X.cpu().numpy().astype(np.float64), D.cpu().numpy().astype(np.float64)
+    assert len(X) > 1000
+    rows = np.random.default_rng(0).choice(len(X), 200, replace=False)
+    base = orc.initial_state(-87.5)[0]
+    d_orc = np.zeros((len(rows), 38))
+    x0 = np.zeros((len(rows), 38))
+    for r, i in enumerate(rows):
+        s = base.copy()
+        s[REF_INDEX] = X[i, :38]
+        ctype = [orc.ENDO, orc.EPI, orc.MCELL][int(np.argmax(X[i, 41:44]))]
+        m = orc.model("baseline", gks_scale=X[i, 38], pca_scale=X[i, 39], gks_iso_scale=X[i, 40])
+        fine = orc.cells_update(s[None].copy(), [ctype], m, dt=0.02, nsteps=5)[0]
+        coarse = orc.cells_update(s[None].copy(), [ctype], m, dt=0.1, nsteps=1)[0]
+        d_orc[r] = (fine - coarse)[REF_INDEX]
+        x0[r] = X[i, :38]
+    d_gpu = D[rows]
+    # FP32 trajectories against FP64 ones: a few FP32 ulps of the state per
+    # step, plus 5% of the correction itself
+    tol = 0.05 * np.abs(d_orc) + 40 * np.finfo(np.float32).eps * np.maximum(np.abs(x0), 1e-3)
+    bad = np.abs(d_gpu - d_orc) > tol
+    assert bad.mean() < 0.01, (bad.sum(0), np.abs(d_gpu - d_orc).max(0))
+
+
+def _sheet(lq, n=24):
+    sh = lq.geometry.sheet(n, n, s1_cols=3)
+    return sh
+
+
+def test_macro_step_applies_network_correction(lq, orc, torch, net):
+    """A uniform sheet in the plateau (no diffusion): after one macro step the
+    difference between the surrogate run and the coarse-only run is the
+    network's correction, as the separate tcgen05 inference kernel computes
+    it from the same state."""
+    from lqt1_gb300 import surrogate as S
+    m = lq.model("baseline", gks_scale=0.5, pca_scale=2.0, gks_iso_scale=1.5)
+    # plateau state of an endocardial cell: 150 ms after a stimulus
+    st = orc.initial_state(-87.5)
+    om = orc.model("baseline", gks_scale=0.5, pca_scale=2.0, gks_iso_scale=1.5)
+    ist = np.array([-52.0])
+    orc.cells_update(st, [orc.ENDO], om, dt=0.02, ist=ist, nsteps=100)
+    orc.cells_update(st, [orc.ENDO], om, dt=0.02, nsteps=7400)
+    sh = _sheet(lq)
+    types = np.where(sh.types == 255, 255, orc.ENDO).astype(np.uint8)
+    runs = {}
+    for mode in ("net", "coarse"):
+        sim = lq.Sim(types, 0.15, precision=lq.MIXED, model=m)
+        sim.set_state(np.repeat(st, sim.n, 0))
+        sim.set_surrogate(net, use_net=(mode == "net"))
+        sim.step(5)                               # plain steps (no V history at step 0)
+        s5 = sim.get_state()
+        sim.step(5)                               # one macro step
+        runs[mode] = (s5, sim.get_state(), sim.surrogate_stats())
+    s5, n10, stn = runs["net"]
+    _, c10, stc = runs["coarse"]
+    assert stn["offered"] == stn["accepted"] == len(s5)
+    # expected correction from the inference kernel
+    x = np.zeros((len(s5), 44), np.float32)
+    x[:, :38] = s5[:, REF_INDEX]
+    x[:, 38:41] = (0.5, 2.0, 1.5)
+    x[:, 41] = 1.0                                # endo
+    L = S._bind_sur()
+    xd = torch.from_numpy(x).cuda()
+    xb = torch.empty((len(x), 48), dtype=torch.bfloat16, device="cuda")
+    y = torch.empty((len(x), 48), dtype=torch.float32, device="cuda")
+    L.lqt_sur_prepare(net._h, xd.data_ptr(), None, None, len(x), xb.data_ptr(), None)
+    net.infer(xb, y)
+    corr = y.cpu().numpy()[:, :38] * net.norm_out[:38]
+    got = (n10 - c10)[:, REF_INDEX]
+    scale = net.norm_out[:38].astype(np.float64)
+    # the fused kernel's packed BF16 SiLU against the FP32 SiLU of the
+    # inference kernel: a few percent of one output standard deviation, plus
+    # the FP32 rounding of the state the correction is added to (V moves
+    # through five substeps)
+    eps = np.finfo(np.float32).eps
+    ulps = np.full(38, 4.0)
+    ulps[0] = 20.0
+    tol = 0.05 * scale + ulps * eps * np.abs(c10[:, REF_INDEX])
+    bad = np.abs(got - corr) > tol
+    assert not bad.any(), (bad.sum(0), (np.abs(got - corr) / scale).max(0))
+    assert np.abs(corr / scale).max() > 0.01     # the correction is not trivially zero
+
+
+def _apd_stats(d, ref):
+    a, ar = d["apd90"], ref["apd90"]
+    both = (a > 0) & (ar > 0)
+    e = np.abs(a - ar)[both]
+    ta = np.abs(d["t_act"] - ref["t_act"])[(d["t_act"] >= 0) & (ref["t_act"] >= 0)]
+    return dict(apd_max=float(e.max()), apd_mean=float(e.mean()), act_max=float(ta.max()), n=int(both.sum()))
+
+
+def test_network_reduces_coarse_step_error(lq, torch, net):
+    """What the trained network gains over the coarse step alone, per macro
+    step, on pairs it has not seen (a fresh seed): the error of the coarse
+    state against 5 plain steps, with and without the network's correction."""
+    from lqt1_gb300 import surrogate as S
+    X, D = S.generate(ncells=4096, cap=400_000, prob=0.01, seed=97)
+    val = S.validate(net, X, D)
+    ratio = val["rmse"] / val["zero_rmse"]
+    assert np.median(ratio) < 0.15, ratio
+    assert ratio[0] < 0.5, ratio                  # V
+    assert (ratio < 1.0).all(), ratio
+
+
+def test_accuracy_against_fp64(lq, torch, net):
+    """2D sheet (120 x 120 at 0.15 mm, one S1 beat, 600 ms): with the
+    surrogate, activation within 0.1 ms and APD90 within 1 ms of the FP64 form
+    at every voxel, V within 0.5 mV outside the upstroke; the coarse step
+    without the network is held to the same bars."""
+    sh = lq.geometry.sheet(120, 120, s1_cols=3)
+    m = lq.model("lqt1", gks_scale=0.5)
+
+    def run(prec, mode):
+        sim = lq.Sim(sh.types, 0.15, precision=prec, model=m)
+        sim.set_protocol(bcl=1000.0, s1_mask=sh.s1_mask, s1_start=0.0, s1_duration=2.0, s1_strength=-52.0,
+                         s1_beats=1)
+        if mode != "plain":
+            sim.set_surrogate(net, use_net=(mode == "net"))
+        vs = []
+        for _ in range(30):
+            sim.step(1000)
+            vs.append(sim.get_v(as_double=True))
+        return sim.detect(), (sim.surrogate_stats() if mode != "plain" else None), sim.check(), np.array(vs)
+
+    ref, _, _, vref = run(lq.FP64, "plain")
+    calm = np.abs(np.diff(vref, axis=0, prepend=vref[:1])) < 1.0
+    for mode in ("net", "coarse"):
+        d, st, bad, v = run(lq.MIXED, mode)
+        e = _apd_stats(d, ref)
+        assert bad == 0
+        assert e["n"] == (ref["apd90"] > 0).sum() > 0.99 * len(ref["apd90"])
+        assert e["act_max"] <= 0.1 + 1e-4, (mode, e)
+        assert e["apd_max"] <= 1.0, (mode, e)
+        assert np.abs(v - vref)[calm].max() < 0.5, mode
+        assert st["accepted"] >= 0.95 * st["offered"] > 0.5 * st["macro_steps"] * len(ref["apd90"])
+
+
+def test_speed_gain_over_plain_step(lq, torch, net):
+    """3D ventricle shell (about 1M voxels), plateau and repolarisation: the
+    surrogate form advances more cell-steps per second than the plain mixed
+    form (same kernels' correctness covered above)."""
+    v = lq.geometry.ventricle(nx=170, ny=170, nz=220, a_out=14.0, c_out=36.0, wall=6.0, z_base=40.0,
+                              island_radius=4.0, stim_radius=2.0)
+    m = lq.model("baseline", gks_scale=0.5, pca_scale=2.0, gks_iso_scale=1.5)
+    rates = {}
+    for mode in ("plain", "net"):
+        sim = lq.Sim(v.types, 0.2, fibre=v.fibre, precision=lq.MIXED, model=m)
+        sim.set_protocol(bcl=800.0, s1_mask=v.s1_mask, s1_start=0.0, s1_duration=2.0, s1_strength=-52.0,
+                         s1_beats=1)
+        sim.tune(3)
+        if mode == "net":
+            sim.set_surrogate(net)
+        sim.step(5000)                            # through the upstroke into the plateau
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim.step(10000)
+        rates[mode] = sim.n * 10000 / (time.perf_counter() - t0)
+    assert rates["net"] > 1.3 * rates["plain"], rates
