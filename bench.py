@@ -7,12 +7,16 @@ every 50 steps.  The metric is cell-steps/s (voxels x steps / s).
 
 Default: 3D truncated prolate-ellipsoid shell in a 320x320x420 grid at
 0.2 mm (about 7.1M tissue voxels), fibres +60 -> -60 degrees, IKs x0.5,
-beta-adrenergic ICaL x2 / IKs x1.5, apical stimulus at BCL 800 ms; the mixed
-form (FP32 gates/currents/diffusion, FP64 concentrations).  The plain FP64
-form is timed on the same state and reported beside it.
+beta-adrenergic ICaL x2 / IKs x1.5, apical stimulus at BCL 800 ms, timed over
+one whole beat (40000 steps).  The headline form is FP32 + learned surrogate
+(0.1 ms macro steps of a coarse TPORd step plus a BF16 tensor-core network's
+correction where |dV/dt| <= 1 mV/ms; plain steps elsewhere).  Beside it: the
+plain mixed form over the same steps, the plain FP64 form, the APD90 /
+activation error of both FP32 forms against FP64 on a 100k-voxel shell over a
+beat, the batched sweep, and the CPU oracle on a slab of the workload.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload ventricle3d|sheet2d]
+                  [--workload ventricle3d|ventricle3d_small|sheet2d]
 
 Under torchrun each rank runs an independent replica (the path has no data
 exchange between instances); value = voxel-steps of all ranks / max time.
@@ -36,11 +40,17 @@ sys.path.insert(0, ROOT)
 METRIC = "monodomain cell-steps/s: plain FP64 vs FP32/surrogate form at ≤1 ms APD90 err"
 UNIT = "cell-steps/s"
 # algorithmic bytes per voxel-step of the fused step kernel (k_grid_step):
-# state read+write (8 FP64 concentrations, 29 evolving gates/fluxes), own V
-# read + write, tissue->grid index, control byte, diffusion tensor (6) and its
-# divergence (3), AP-detector record (16 B read)
+# state read+write (8 concentrations as Kahan FP32 pairs or FP64, 29 evolving
+# gates/fluxes), own V read + write, tissue->grid index, control byte,
+# diffusion tensor (6) and its divergence (3), AP-detector record (16 B read)
 BYTES_MIXED = 8 * 8 * 2 + 29 * 4 * 2 + 4 + 4 + 4 + 1 + 9 * 4 + 16
 BYTES_FP64 = 8 * 8 * 2 + 29 * 8 * 2 + 8 + 8 + 4 + 1 + 9 * 8 + 16
+# surrogate macro-step kernel (k_sur_grid), per voxel per launch: V now and
+# one step back, grid index, control byte, detector record, the state read
+# once and written once (8 Kahan pairs + 29 gates), the macro step's rate
+BYTES_SUR_MACRO = 4 + 4 + 4 + 1 + 16 + (8 * 8 + 29 * 4) * 2 + 4
+# and the network's multiply-adds (48 -> 128 -> 128 -> 48) per voxel
+FLOP_SUR_MACRO = 2 * (48 * 128 + 128 * 128 + 128 * 48)
 
 
 def workload_model():
@@ -122,9 +132,9 @@ def measured_peaks():
         return {}
 
 
-def traffic_summary():
-    """Per-launch DRAM bytes of k_grid_step from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "k_grid_step_ventricle3d.json")
+def traffic_summary(name):
+    """Per-launch DRAM bytes of a kernel from its committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", name)
     try:
         d = json.load(open(p))
         return d.get("traffic_bytes_per_launch_full_workload")
@@ -185,12 +195,14 @@ def cpu_model_name():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=500)
-    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=40000, help="timed steps (default: one 800 ms beat)")
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ventricle3d", choices=["ventricle3d", "ventricle3d_small", "sheet2d"])
-    ap.add_argument("--prerun", type=int, default=1000, help="untimed steps to start the wave (setup)")
+    ap.add_argument("--prerun", type=int, default=0, help="untimed steps before the timed region (setup)")
     ap.add_argument("--fp64-steps", type=int, default=10)
+    ap.add_argument("--mixed-steps", type=int, default=-1, help="steps of the plain mixed leg (-1 = --steps)")
+    ap.add_argument("--no-accuracy", dest="accuracy", action="store_false")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sweep-beats", type=int, default=2,
                     help="beats of the 4096-instance batched sweep leg (0 = skip; 20 = the full sweep)")
@@ -220,6 +232,7 @@ def main():
 
     import torch
     import lqt1_gb300 as lq
+    from lqt1_gb300 import surrogate as S
 
     if world > 1:
         import torch.distributed as dist
@@ -228,48 +241,72 @@ def main():
     dev = torch.cuda.current_device()
     w = build_workload(args.workload)
     stream = torch.cuda.Stream()
-    sim = lq.Sim(w["types"], w["dx"], fibre=w["fibre"], precision=lq.MIXED, model=workload_model(), detect=True,
-                 vmin_ok=-200.0, vmax_ok=200.0, stream=stream.cuda_stream)
-    sim.set_protocol(bcl=w["bcl"], s1_mask=w["s1"], s1_start=0.0, s1_duration=2.0, s1_strength=-52.0, s1_beats=3,
-                     s2_time=-1.0)
-    sim.set_electrodes(np.array(w["electrodes"]), every=50)
-    n = sim.n
-    sim.step(args.prerun)
-    variant, tune_ms = sim.tune(-1)          # occupancy variant of the step kernel
-    sim.step(args.warmup)
-    torch.cuda.synchronize()
+    net = S.load(stream=stream.cuda_stream)
+
+    def make_sim(precision, surrogate):
+        sim = lq.Sim(w["types"], w["dx"], fibre=w["fibre"], precision=precision, model=workload_model(),
+                     detect=True, vmin_ok=-200.0, vmax_ok=200.0, stream=stream.cuda_stream)
+        sim.set_protocol(bcl=w["bcl"], s1_mask=w["s1"], s1_start=0.0, s1_duration=2.0, s1_strength=-52.0,
+                         s1_beats=3, s2_time=-1.0)
+        sim.set_electrodes(np.array(w["electrodes"]), every=50)
+        if surrogate:
+            sim.set_surrogate(net)
+        return sim
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
 
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(dev) as clk:
+    def timed(sim, steps, clk=None):
+        """CUDA-event time of `steps` steps on the simulation's stream, max over ranks."""
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         barrier()
         torch.cuda.synchronize()
         e0.record(stream)
-        sim.step(args.steps)
+        sim.step(steps)
         e1.record(stream)
         torch.cuda.synchronize()
         barrier()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    # ---- headline: FP32 + surrogate form -----------------------------------
+    sim = make_sim(lq.MIXED, True)
+    n = sim.n
+    sim.step(args.prerun)
+    variant, tune_ms = sim.tune(-1)          # occupancy variant of the plain step kernel
+    sim.step(args.warmup)
+    sim.surrogate_stats(reset=True)
+    with ClockSampler(dev) as clk:
+        ms = timed(sim, args.steps)
     value = world * n * args.steps / (ms / 1e3)
     nbad = sim.check()
-
-    # roofline of the dominant kernel: per-launch CUDA-event time of k_grid_step
-    ms_step, ms_ghost, _ = sim.profile(20)
+    sst = sim.surrogate_stats()
+    ms_sub, ms_ghost_s, ms_sur = sim.profile(10)
     peaks = measured_peaks()
     peak = peaks.get("hbm_gbs")
     peak_kind = "measured" if peak else "fallback"
     peak = peak or 6800.0
-    achieved = BYTES_MIXED * n / (ms_step / 1e3) / 1e9
-    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": traffic_summary(), "kernel": "k_grid_step<float,3>", "kernel_ms": ms_step,
-            "bytes_per_cell_step": BYTES_MIXED, "peak_source": peak_kind}
+    tpeak = peaks.get("bf16_tflops_sustained") or peaks.get("bf16_tflops") or 1700.0
+    # dominant kernel of the surrogate form: the macro-step kernel (one launch
+    # per 5 steps), algorithmic bytes and tensor FLOPs per voxel per launch
+    ach_sur = BYTES_SUR_MACRO * n / (ms_sur / 1e3) / 1e9
+    roof = {"bound": "hbm", "achieved": ach_sur, "peak": peak, "unit": "GB/s", "frac": ach_sur / peak,
+            "traffic": traffic_summary("k_sur_grid_ventricle3d.json"), "kernel": "k_sur_grid", "kernel_ms": ms_sur,
+            "bytes_per_voxel_launch": BYTES_SUR_MACRO, "peak_source": peak_kind,
+            "tensor": {"achieved_tflops": FLOP_SUR_MACRO * n / (ms_sur / 1e3) / 1e12, "peak_tflops": tpeak,
+                       "frac": FLOP_SUR_MACRO * n / (ms_sur / 1e3) / 1e12 / tpeak,
+                       "flop_per_voxel_launch": FLOP_SUR_MACRO},
+            "substep": {"kernels": "k_sur_substep + k_grid_step over the plain-voxel list", "ms": ms_sub,
+                        "ghost_ms": ms_ghost_s}}
+    surrogate = {"macro_steps": sst["macro_steps"], "voxel_offers": sst["offered"], "accepted": sst["accepted"],
+                 "accepted_frac_of_voxel_macro_steps": sst["accepted"] / max(1, sst["macro_steps"] * n),
+                 "wait_timeouts": sst["wait_timeouts"], "network": {k: net.meta.get(k) for k in
+                                                                   ("pairs", "epochs", "train_s", "gen_s")}}
 
     # e2e through the C ABI with pinned host buffers: initial state H2D, then
     # every step lqt_sim_step + lqt_sim_get_v (the reference's host loop
@@ -287,28 +324,48 @@ def main():
     sim.get_state(out=st_host)
     t_e2e = time.perf_counter() - t0
     e2e = {"value": world * n * k_e2e / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(n * 320 / k_e2e),
-           "d2h_bytes_per_step": int(n * 4 + n * 320 / k_e2e), "steps": k_e2e}
+           "d2h_bytes_per_step": int(n * 4 + n * 320 / k_e2e), "steps": k_e2e, "form": "FP32 + surrogate"}
+    sim.close()
 
-    # plain FP64 form on the same state
+    # ---- plain mixed form over the same steps ------------------------------
+    mixed = None
+    if args.mixed_steps != 0:
+        ksteps = args.steps if args.mixed_steps < 0 else args.mixed_steps
+        sm = make_sim(lq.MIXED, False)
+        sm.step(args.prerun)
+        variant_m, tune_m = sm.tune(-1)
+        sm.step(args.warmup)
+        ms_m = timed(sm, ksteps)
+        ms_step, ms_ghost, _ = sm.profile(20)
+        ach = BYTES_MIXED * n / (ms_step / 1e3) / 1e9
+        mixed = {"value": world * n * ksteps / (ms_m / 1e3), "unit": UNIT, "steps": ksteps,
+                 "surrogate_over_mixed": value / (world * n * ksteps / (ms_m / 1e3)),
+                 "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                              "traffic": traffic_summary("k_grid_step_ventricle3d.json"),
+                              "kernel": "k_grid_step<float,3>", "kernel_ms": ms_step,
+                              "bytes_per_cell_step": BYTES_MIXED, "peak_source": peak_kind},
+                 "step_kernel_variant": {"min_ctas_per_sm": variant_m,
+                                         "tuned_ms": [round(float(x), 4) for x in tune_m[:3]]},
+                 "blowup_voxel_steps": sm.check()}
+        sm.close()
+
+    # ---- plain FP64 form on the same state ----------------------------------
     fp64 = None
     if args.fp64_steps > 0:
-        s64 = lq.Sim(w["types"], w["dx"], fibre=w["fibre"], precision=lq.FP64, model=workload_model(), detect=True,
-                     stream=stream.cuda_stream)
-        s64.set_protocol(bcl=w["bcl"], s1_mask=w["s1"], s1_start=0.0, s1_duration=2.0, s1_strength=-52.0,
-                         s1_beats=3)
+        s64 = make_sim(lq.FP64, False)
         s64.set_state(st_host)
         s64.step(2)
-        torch.cuda.synchronize()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        s64.step(args.fp64_steps)
-        b.record(stream)
-        torch.cuda.synchronize()
-        v64 = n * args.fp64_steps / (a.elapsed_time(b) / 1e3)
+        ms64t = timed(s64, args.fp64_steps)
+        v64 = n * args.fp64_steps / (ms64t / 1e3)
         ms64, _, _ = s64.profile(2)
         fp64 = {"value": v64 * world, "unit": UNIT, "steps": args.fp64_steps, "kernel_ms": ms64,
-                "achieved_gbs": BYTES_FP64 * n / (ms64 / 1e3) / 1e9, "mixed_over_fp64": value / (v64 * world)}
+                "achieved_gbs": BYTES_FP64 * n / (ms64 / 1e3) / 1e9, "surrogate_over_fp64": value / (v64 * world)}
         s64.close()
+
+    # ---- accuracy of the surrogate form against the FP64 form ----------------
+    accuracy = None
+    if args.accuracy:
+        accuracy = accuracy_leg(lq, net, stream)
 
     # batched sweep leg: 4096 uneven single cells / strands (50-400 cells), own
     # parameters each, one persistent graph-captured launch (autotuned shape)
@@ -333,19 +390,59 @@ def main():
                "sample": f"{r['n']} tissue voxels (x-slab of the workload), {r['steps']} steps, FP64 oracle, "
                          f"OpenMP on {r['cores']} threads, {cpu_model_name()}"}
     clocks = clk.summary()
-    ecg_launches = 2 * (args.steps // 50)
+    # our kernels in the timed region: per step the V-only substep, the plain
+    # step over the listed voxels and the ghost/clock kernel; per 5 steps the
+    # macro-step kernel; per 50 steps the two ECG kernels
+    launches = 3 * args.steps + args.steps // 5 + 2 * (args.steps // 50)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": w["desc"], "tissue_voxels": n, "form": "mixed (FP32 gates/currents/diffusion, "
-                       "FP64 concentrations)", "dt_ms": 0.02, "electrodes": len(w["electrodes"]),
-                       "l2": "inputs larger than L2 (state %.2f GB/step)" % (BYTES_MIXED * n / 1e9),
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": w["desc"], "tissue_voxels": n,
+                       "form": "FP32 + learned surrogate (FP32 gates/currents/diffusion, Kahan-compensated FP32 "
+                               "concentrations; 0.1 ms macro steps of a coarse TPORd step + BF16 tcgen05 MLP "
+                               "correction where |dV/dt| <= 1 mV/ms, plain 0.02 ms steps elsewhere)",
+                       "dt_ms": 0.02, "t_ms": [round((args.prerun + args.warmup + 15) * 0.02, 2),
+                                               round((args.prerun + args.warmup + 15 + args.steps) * 0.02, 2)],
+                       "electrodes": len(w["electrodes"]),
+                       "l2": "inputs larger than L2 (state %.2f GB)" % (BYTES_MIXED * n / 1e9),
                        "parallelism": f"replicas x{world}",
                        "step_kernel_variant": {"min_ctas_per_sm": variant,
                                                "tuned_ms": [round(float(x), 4) for x in tune_ms[:3]]}},
-            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "fp64_form": fp64, "batched_sweep": sweep,
-            "gpu_launches": 2 * args.steps + ecg_launches, "clocks": clocks, "blowup_voxel_steps": nbad}
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "surrogate": surrogate, "mixed_form": mixed,
+            "fp64_form": fp64, "accuracy": accuracy, "batched_sweep": sweep, "gpu_launches": launches,
+            "clocks": clocks, "blowup_voxel_steps": nbad}
     print(json.dumps(line), flush=True)
+
+
+def accuracy_leg(lq, net, stream):
+    """APD90 and activation-time error of the surrogate form (and of the plain
+    mixed form) against the FP64 form: 100k-voxel ventricle shell of the same
+    construction, same model, one S1 beat (790 ms)."""
+    v = lq.geometry.ventricle(nx=64, ny=64, nz=84, a_out=5.8, c_out=14.0, wall=3.0, z_base=15.5, island_radius=2.0,
+                              stim_radius=1.2)
+    nsteps = 39500
+    out = {"workload": "3d-ventricle 64x64x84 @0.2mm, %d tissue voxels, 1 beat" % int((v.types != 255).sum())}
+    res = {}
+    for name, prec, sur in (("fp64", lq.FP64, False), ("mixed", lq.MIXED, False), ("surrogate", lq.MIXED, True)):
+        sim = lq.Sim(v.types, 0.2, fibre=v.fibre, precision=prec, model=workload_model(), stream=stream.cuda_stream)
+        sim.set_protocol(bcl=800.0, s1_mask=v.s1_mask, s1_start=0.0, s1_duration=2.0, s1_strength=-52.0,
+                         s1_beats=1)
+        if sur:
+            sim.set_surrogate(net)
+        sim.step(nsteps)
+        res[name] = sim.detect()
+        sim.close()
+    ref = res["fp64"]
+    for name in ("mixed", "surrogate"):
+        d = res[name]
+        both = (d["apd90"] > 0) & (ref["apd90"] > 0)
+        ea = np.abs(d["apd90"] - ref["apd90"])[both]
+        act = (d["t_act"] >= 0) & (ref["t_act"] >= 0)
+        et = np.abs(d["t_act"] - ref["t_act"])[act]
+        out[name] = {"apd90_max_ms": float(ea.max()), "apd90_mean_ms": float(ea.mean()),
+                     "activation_max_ms": float(et.max()), "voxels_compared": int(both.sum()),
+                     "voxels_missing": int((~both).sum())}
+    return out
 
 
 if __name__ == "__main__":

@@ -78,6 +78,7 @@ struct lqt_sim {
     lqt_mlp *sur = nullptr;
     lqt_sur_config sur_cfg{};
     float *srate = nullptr;
+    uint8_t *sdflag = nullptr;
     int32_t *plist = nullptr;
     unsigned long long *plist_n = nullptr;
     bool plist_valid = false;       // rate/list written by a macro-step launch still in effect
@@ -141,6 +142,7 @@ struct lqt_sim {
         g.nbad = nbad;
         const bool in_macro = sur && plist_valid;
         g.srate = in_macro ? srate : nullptr;
+        g.sdflag = in_macro ? sdflag : nullptr;
         g.plist = in_macro ? plist : nullptr;
         g.plist_n = in_macro ? (const int64_t *)plist_n : nullptr;
         return g;
@@ -223,6 +225,7 @@ int launch_sur_if_due(lqt_sim *s)
     SurGrid sg{};
     if (!mlp_device_view(s->sur, &sg.w, &sg.norm)) return fail(LQT_ERR_STATE, "surrogate network has no parameters");
     sg.rate = s->srate;
+    sg.dflag = s->sdflag;
     sg.plist = s->plist;
     sg.plist_n = s->plist_n;
     sg.stats = s->sur_stats;
@@ -297,8 +300,11 @@ int step_once(lqt_sim *s)
 }
 
 // Autotuner: time `per` real steps with each occupancy variant of the step
-// kernel (CUDA events around the step kernel only) and keep the fastest.  The
-// variants differ only in register allocation, so the steps are valid
+// kernels (CUDA events around the step kernels only) and keep the fastest.
+// The variants take turns step by step, so each sees the same phases of the
+// simulation (with a surrogate attached, the share of plain voxels changes
+// from one macro step to the next); the first round only loads the modules.
+// The variants differ only in register allocation, so the steps are valid
 // simulation steps whichever variant runs them.  Returns the steps consumed.
 int autotune(lqt_sim *s, int per, int64_t *consumed)
 {
@@ -307,14 +313,12 @@ int autotune(lqt_sim *s, int per, int64_t *consumed)
     cudaEvent_t a, b;
     CK(cudaEventCreate(&a));
     CK(cudaEventCreate(&b));
-    float best = 1e30f;
-    int best_m = cand[0];
+    float tot[4] = {0, 0, 0, 0};
     int rc = LQT_OK;
     *consumed = 0;
-    for (int c = 0; c < ncand && rc == LQT_OK; ++c) {
-        s->minb = cand[c];
-        float tot = 0.f;
-        for (int i = 0; i < per && rc == LQT_OK; ++i) {
+    for (int i = 0; i < per && rc == LQT_OK; ++i) {
+        for (int c = 0; c < ncand && rc == LQT_OK; ++c) {
+            s->minb = cand[c];
             rc = launch_sur_if_due(s);
             if (rc) break;
             cudaError_t e = cudaEventRecord(a, s->stream);
@@ -333,10 +337,14 @@ int autotune(lqt_sim *s, int per, int64_t *consumed)
             s->time += s->p.dt;
             ++*consumed;
             if (s->nel > 0 && s->ecg_every > 0 && s->step % s->ecg_every == 0) rc = launch_ecg_now(s);
-            if (i > 0) tot += ms;     // the first launch of a variant pays its module load
+            if (i > 0) tot[c] += ms;
         }
-        const float avg = per > 1 ? tot / (per - 1) : tot;
-        if (c < 4) s->tune_ms[c] = avg;
+    }
+    float best = 1e30f;
+    int best_m = cand[0];
+    for (int c = 0; c < ncand; ++c) {
+        const float avg = per > 1 ? tot[c] / (per - 1) : tot[c];
+        s->tune_ms[c] = avg;
         if (avg < best) {
             best = avg;
             best_m = cand[c];
@@ -948,6 +956,7 @@ int lqt_sim_set_surrogate(lqt_sim *s, lqt_mlp *m, const lqt_sur_config *cfg)
     if (!s->srate) {
         int rc = s->mem.alloc((void **)&s->srate, s->ntissue * 4) |
                  s->mem.alloc((void **)&s->plist, s->ntissue * 4) |
+                 s->mem.alloc((void **)&s->sdflag, s->ntissue) |
                  s->mem.alloc((void **)&s->plist_n, sizeof(unsigned long long)) |
                  s->mem.alloc((void **)&s->sur_stats, 2 * sizeof(unsigned long long)) |
                  s->mem.alloc((void **)&s->sur_err, sizeof(int));

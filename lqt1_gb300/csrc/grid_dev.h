@@ -56,6 +56,7 @@ template <typename R> struct GridDev {
     // for the current macro step, or NaN where the plain step runs; and the
     // list of the voxels that run the plain step (plist_n entries); null = off
     const float *srate;
+    const uint8_t *sdflag;         // 1 = the voxel's detector runs during the macro step
     const int32_t *plist;
     const int64_t *plist_n;
 };

@@ -172,65 +172,88 @@ __global__ void __launch_bounds__(256, MINB) k_grid_step(GridDev<R> gd, StepT<R>
 
 // Inside a surrogate macro step: the voxels whose ionic change is fixed
 // (srate not NaN) move V by it plus diffusion, in the update form of
-// TPORd.cc:928-930; the others are left to k_grid_step over plist.  Every
-// per-voxel load that depends only on k (rate, grid index, control byte,
-// diffusion tensor, detector record) is issued before the first use, so a
-// voxel costs two memory round trips (those, then the V stencil).
+// TPORd.cc:928-930; the others are left to k_grid_step over plist.  A thread
+// takes kSubU voxels (k and k + blockDim.x ...), and every load that depends
+// only on k (rate, grid index, control and detector flags, diffusion tensor)
+// is issued before the first use, so the loads of both voxels overlap in two
+// memory round trips (those, then the V stencils).  The detector record is
+// read only where the macro-step kernel flagged that it can change.
+constexpr int kSubU = 2;
+
+template <int DIM>
+__device__ __forceinline__ float sub_du(const GridDev<float> &gd, const float *__restrict__ V, int64_t g, int64_t k,
+                                        float vc, const float *Dt, const float *Bt)
+{
+    if (DIM == 1 || !gd.d6) return grid_du<float, DIM>(gd, V, g, k, vc);
+    // the anisotropic stencil of grid_du with the tensor already loaded
+    const int64_t sx = gd.sx, sy = gd.sy;
+    const float vxp = V[g + sx], vxm = V[g - sx], vyp = V[g + sy], vym = V[g - sy];
+    const float c2 = gd.inv_dx2, c4 = gd.inv_4dx2, c1 = gd.inv_2dx;
+    const float lxx = (vxp + vxm - 2.f * vc) * c2;
+    const float lyy = (vyp + vym - 2.f * vc) * c2;
+    const float lxy = (V[g + sx + sy] + V[g - sx - sy] - V[g - sx + sy] - V[g + sx - sy]) * c4;
+    float du = Dt[0] * lxx + Dt[1] * lyy + 2.f * Dt[3] * lxy + Bt[0] * ((vxp - vxm) * c1) + Bt[1] * ((vyp - vym) * c1);
+    if constexpr (DIM == 3) {
+        const float vzp = V[g + 1], vzm = V[g - 1];
+        const float lzz = (vzp + vzm - 2.f * vc) * c2;
+        const float lxz = (V[g + sx + 1] + V[g - sx - 1] - V[g - sx + 1] - V[g + sx - 1]) * c4;
+        const float lyz = (V[g + sy + 1] + V[g - sy - 1] - V[g - sy + 1] - V[g + sy - 1]) * c4;
+        du += Dt[2] * lzz + 2.f * (Dt[4] * lxz + Dt[5] * lyz) + Bt[2] * ((vzp - vzm) * c1);
+    }
+    return du;
+}
+
 template <int DIM> __global__ void __launch_bounds__(256) k_sur_substep(GridDev<float> gd, float dt, int cur)
 {
-    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (k >= gd.ntissue) return;
-    const float r = gd.srate[k];
-    const int64_t g = DIM == 1 ? k : (int64_t)gd.gidx[k];
-    const uint8_t ctl = gd.ctl[k];
-    float Dt[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, Bt[3] = {0.f, 0.f, 0.f};
+    const int64_t k0 = blockIdx.x * (int64_t)(blockDim.x * kSubU) + threadIdx.x;
     const bool aniso = DIM > 1 && gd.d6;
-    if (aniso) {
+    float r[kSubU], Dt[kSubU][6], Bt[kSubU][3];
+    int64_t g[kSubU];
+    uint8_t ctl[kSubU], fl[kSubU];
+    bool on[kSubU];
 #pragma unroll
-        for (int i = 0; i < (DIM == 3 ? 6 : 4); ++i) Dt[i] = __ldg(gd.d6 + 6 * k + i);
+    for (int u = 0; u < kSubU; ++u) {
+        const int64_t k = k0 + u * (int64_t)blockDim.x;
+        on[u] = k < gd.ntissue;
+        r[u] = on[u] ? gd.srate[k] : __int_as_float(0x7fc00000);
+        g[u] = on[u] ? (DIM == 1 ? k : (int64_t)gd.gidx[k]) : 0;
+        ctl[u] = on[u] ? gd.ctl[k] : 0;
+        fl[u] = on[u] && gd.det ? gd.sdflag[k] : 0;
 #pragma unroll
-        for (int i = 0; i < (DIM == 3 ? 3 : 2); ++i) Bt[i] = __ldg(gd.b3 + 3 * k + i);
+        for (int i = 0; i < 6; ++i) Dt[u][i] = 0.f;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) Bt[u][i] = 0.f;
+        if (aniso && on[u]) {
+#pragma unroll
+            for (int i = 0; i < (DIM == 3 ? 6 : 4); ++i) Dt[u][i] = __ldg(gd.d6 + 6 * k + i);
+#pragma unroll
+            for (int i = 0; i < (DIM == 3 ? 3 : 2); ++i) Bt[u][i] = __ldg(gd.b3 + 3 * k + i);
+        }
     }
-    float4 det = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (gd.det) det = gd.det[k];
-    if (!(r == r)) return;
+    bool any = false;
+#pragma unroll
+    for (int u = 0; u < kSubU; ++u) {
+        on[u] = on[u] && r[u] == r[u];
+        any |= on[u];
+    }
+    if (!any) return;
     const Clock ck = *gd.clk;
     const float *__restrict__ V = gd.vg[cur];
     float *__restrict__ Vn = gd.vg[cur ^ 1];
-    const float vc = V[g];
-    float du;
-    if (DIM == 1 || !aniso) {
-        du = grid_du<float, DIM>(gd, V, g, k, vc);
-    } else {
-        // the anisotropic stencil of grid_du with the tensor already loaded
-        const int64_t sx = gd.sx, sy = gd.sy;
-        const float vxp = V[g + sx], vxm = V[g - sx], vyp = V[g + sy], vym = V[g - sy];
-        const float lxy0 = V[g + sx + sy], lxy1 = V[g - sx - sy], lxy2 = V[g - sx + sy], lxy3 = V[g + sx - sy];
-        float vzp = 0.f, vzm = 0.f, z0 = 0.f, z1 = 0.f, z2 = 0.f, z3 = 0.f, y0 = 0.f, y1 = 0.f, y2 = 0.f, y3 = 0.f;
-        if constexpr (DIM == 3) {
-            vzp = V[g + 1];
-            vzm = V[g - 1];
-            z0 = V[g + sx + 1]; z1 = V[g - sx - 1]; z2 = V[g - sx + 1]; z3 = V[g + sx - 1];
-            y0 = V[g + sy + 1]; y1 = V[g - sy - 1]; y2 = V[g - sy + 1]; y3 = V[g + sy - 1];
-        }
-        const float c2 = gd.inv_dx2, c4 = gd.inv_4dx2, c1 = gd.inv_2dx;
-        const float lxx = (vxp + vxm - 2.f * vc) * c2;
-        const float lyy = (vyp + vym - 2.f * vc) * c2;
-        const float lxy = (lxy0 + lxy1 - lxy2 - lxy3) * c4;
-        du = Dt[0] * lxx + Dt[1] * lyy + 2.f * Dt[3] * lxy + Bt[0] * ((vxp - vxm) * c1) + Bt[1] * ((vyp - vym) * c1);
-        if constexpr (DIM == 3) {
-            const float lzz = (vzp + vzm - 2.f * vc) * c2;
-            const float lxz = (z0 + z1 - z2 - z3) * c4;
-            const float lyz = (y0 + y1 - y2 - y3) * c4;
-            du += Dt[2] * lzz + 2.f * (Dt[4] * lxz + Dt[5] * lyz) + Bt[2] * ((vzp - vzm) * c1);
-        }
+#pragma unroll
+    for (int u = 0; u < kSubU; ++u) {
+        if (!on[u]) continue;
+        const int64_t k = k0 + u * (int64_t)blockDim.x;
+        const float vc = V[g[u]];
+        const float du = sub_du<DIM>(gd, V, g[u], k, vc, Dt[u], Bt[u]);
+        const float ist = grid_stim(gd, ck, ctl[u], k);
+        const float dvdt = r[u] - ist;
+        const float vn = vc + (dvdt + du) * dt;
+        Vn[g[u]] = vn;
+        if (fl[u]) grid_detect(gd, ck, k, vc, vn, dvdt);
+        const bool bad = !(vn == vn) || vn < gd.vmin_ok || vn > gd.vmax_ok;
+        if (bad) atomicAdd(gd.nbad, 1ull);
     }
-    const float ist = grid_stim(gd, ck, ctl, k);
-    const float dvdt = r - ist;
-    const float vn = vc + (dvdt + du) * dt;
-    Vn[g] = vn;
-    if (gd.det) grid_detect_rec(gd, ck, k, det, vc, vn, dvdt);
-    grid_count_bad(gd, vn);
 }
 
 // Mirror-boundary refresh of the new grid, then the clock advance for the

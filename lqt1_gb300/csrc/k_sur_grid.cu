@@ -53,6 +53,7 @@ constexpr int kThreads = 128 * kGroups;
 constexpr uint32_t kColsPerGroup = 128;
 constexpr uint32_t kTmemCols = kColsPerGroup * kGroups;   // the SM's 512 columns
 constexpr uint32_t kWaitLimit = 1u << 24;  // bounded mbarrier polls
+constexpr float kDetMargin = 2.f;          // mV a surrogate voxel cannot cover in one macro step
 
 constexpr uint32_t kOffW1 = 0;                                      // 128 x 48
 constexpr uint32_t kOffW2 = kOffW1 + kMlpHid * kMlpIn * 2;          // 128 x 128
@@ -253,12 +254,34 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
     const int64_t ntiles = (nt + kTile - 1) / kTile;
     unsigned long long n_offer = 0, n_acc = 0;
     const int64_t tstride = (int64_t)gridDim.x * kGroups;
+    // an S1 window opens during this macro step: every detector records its rest
+    bool opens = false;
+    {
+        const int32_t nwin = gd.win ? gd.nwin : 0;
+        const int32_t w = ck.widx < 0 ? 0 : ck.widx;
+        for (int32_t i = w; i < nwin && i < w + 2; ++i)
+            opens |= gd.win[i].on >= ck.step && gd.win[i].on < ck.step + sg.nsub;
+    }
 
     // the warpgroups are independent (own tiles, barrier, TMEM columns and
     // operand buffer); the loop is uniform within a warpgroup
     for (int64_t tile = (int64_t)blockIdx.x * kGroups + grp; tile < ntiles; tile += tstride) {
         const int64_t k = tile * kTile + t;
-        bool elig = false;
+        // the next tile's state lines into L2 (one 128-byte line per array
+        // and warp: lane L takes state arrays L and 32 + L)
+        {
+            const int64_t kn = (tile + tstride) * kTile + (warp & 3) * 32;
+            if (kn < nt) {
+                const int64_t ld = gd.s.ld;
+                const float *cf = reinterpret_cast<const float *>(gd.s.conc);
+#pragma unroll
+                for (int a = lane; a < 16 + 29; a += 32) {
+                    const float *p = a < 16 ? cf + a * ld + kn : gd.s.gate + ((a - 16) < 3 ? a - 16 : a - 14) * ld + kn;
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+                }
+            }
+        }
+        bool elig = false, need_det = false;
         float vc = 0.f;
         int ct = 0;
         if (k < nt) {
@@ -268,7 +291,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
             const uint8_t ctl = gd.ctl[k];
             ct = ctl & kCtlType;
             bool rising = false;
-            if (gd.det) rising = (__float_as_uint(gd.det[k].w) & 7u) == kDetRise;
+            if (gd.det) {
+                const float4 d = gd.det[k];
+                const uint32_t ph = __float_as_uint(d.w) & 7u;
+                rising = ph == kDetRise;
+                // does the detector need this voxel's substeps?  A cycle that
+                // opens; an activation crossing within reach; in the fall, the
+                // running peak, the 50% (EAD) and the 90% levels
+                const float amp = d.y - d.x;
+                need_det = opens || (ph == kDetWait && vc > gd.act_thr - kDetMargin) ||
+                           (ph == kDetFall && !(vc < d.y - kDetMargin && vc > d.y - 0.5f * amp + kDetMargin));
+            }
             elig = net_ok && !rising && fabsf(dv) <= sg.dvdt_max && !stim_ahead(gd, ck, ctl, k, sg.nsub);
         }
         // 1. features (the previous tile's MMAs have all completed)
@@ -416,6 +449,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
             if (ok) {
                 store_cell(c, gd.s, k);
                 sg.rate[k] = dvm * inv_mac;
+                sg.dflag[k] = need_det ? 1 : 0;
             }
         }
         const bool plain = k < nt && !ok;

@@ -7,7 +7,7 @@ namespace lqt {
 cudaError_t launch_sur_substep(const GridDev<float> &gd, double dt, int cur, int dim, cudaStream_t st)
 {
     if (gd.ntissue <= 0) return cudaSuccess;
-    const unsigned nb = (unsigned)((gd.ntissue + 255) / 256);
+    const unsigned nb = (unsigned)((gd.ntissue + 256 * kSubU - 1) / (256 * kSubU));
     if (dim == 1) k_sur_substep<1><<<nb, 256, 0, st>>>(gd, (float)dt, cur);
     else if (dim == 2) k_sur_substep<2><<<nb, 256, 0, st>>>(gd, (float)dt, cur);
     else k_sur_substep<3><<<nb, 256, 0, st>>>(gd, (float)dt, cur);

@@ -27,6 +27,7 @@ struct SurGrid {
     MlpDev w;
     const float *norm;              // in_mean[48], in_scale[48], out_scale[48], out_bound[48]
     float *rate;                    // per tissue voxel: ionic dV/dt of the macro step, NaN = plain step
+    uint8_t *dflag;                 // per tissue voxel: 1 = its AP detector runs on the substeps
     int32_t *plist;                 // voxels that run the plain step during the macro step
     unsigned long long *plist_n;    // their count (zero before the launch)
     unsigned long long *stats;      // [0] voxels offered, [1] accepted
