@@ -145,7 +145,8 @@ typedef struct lqt_instance {
     int32_t n_stim;            /* cells [0, n_stim) receive S1 (3 in OneD.cc:340) */
     int32_t model;             /* index into the models array */
     int32_t record;            /* 1 = record V every rec_every steps; strands also
-                                  record the pseudo-ECG at ecg_x0 */
+                                  record the pseudo-ECG at ecg_x0; 3 = also ICaL
+                                  and IKs of the first cell (SingleCell.cc:113-139) */
     double dx;                 /* mm (0.15, OneD.cc:47) */
     double bcl;                /* ms */
     double s1_start;           /* ms into each cycle */
@@ -156,6 +157,17 @@ typedef struct lqt_instance {
     double t_stop;             /* steps run while time <= t_stop (OneD.cc:317) */
     double ecg_x0;             /* electrode, mm from cell 0 (35 in plot1DECG_compare.py:83) */
     double act_threshold;      /* mV (-30, OneD.cc:422) */
+    /* S2 (OneD_VW.cc:265-279): cells [s2_cell0, s2_cell0 + s2_ncells) receive
+     * s2_strength at the steps whose time t has t - s2_base >= s2_offset and
+     * t - s2_base < s2_offset + s2_duration, unless an S1 window is open
+     * (the reference tests S1 first).  s2_ncells = 0: no S2. */
+    double s2_base, s2_offset, s2_duration, s2_strength;
+    int32_t s2_cell0, s2_ncells;
+    /* 1 = keep the maximum V of every cell over the steps with
+     * t - s2_base >= s2_offset, starting from -100 (maxEndo / maxEpi,
+     * OneD_VW.cc:246-247,340-344); read with lqt_batch_get_vmax. */
+    int32_t track_vmax;
+    int32_t reserved1;         /* must be zero */
 } lqt_instance;
 
 typedef struct lqt_batch_params {
@@ -187,8 +199,13 @@ int lqt_batch_run(lqt_batch *b);
 int lqt_batch_get_detect(lqt_batch *b, float *t_act, float *apd90,
                          float *dvdt_max, uint8_t *ead, int32_t *nbeats);
 /* Recorded V of instance i ([nrec][ncells]), record times and pseudo-ECG. */
-int lqt_batch_get_record(lqt_batch *b, int32_t inst, float *v, double *t,
+int lqt_batch_get_record(lqt_batch *b, int32_t inst, double *v, double *t,
                          double *ecg, int64_t cap, int64_t *nrec);
+/* ICaL and IKs of the first cell at the same records (record = 3). */
+int lqt_batch_get_record_currents(lqt_batch *b, int32_t inst, double *ical,
+                                  double *iks, int64_t cap, int64_t *nrec);
+/* Per cell (input order): the maximum V of the track_vmax watch. */
+int lqt_batch_get_vmax(lqt_batch *b, float *vmax_host);
 int lqt_batch_get_state(lqt_batch *b, double *state_host);
 int lqt_batch_set_state(lqt_batch *b, const double *state_host);
 /* The launch configuration the autotuner chose (threads = 0 in the params):
@@ -341,6 +358,79 @@ int lqt_sim_check(lqt_sim *s, int64_t *n_bad);
 /* Binary checkpoint: header + version + per-state arrays. */
 int lqt_sim_checkpoint(lqt_sim *s, const char *path);
 int lqt_sim_restore(lqt_sim *s, const char *path);
+
+/* ======================================================================== *
+ *  Output files in the reference drivers' formats.
+ * ======================================================================== */
+
+/* V on the lattice of every `stride`-th voxel per axis of a 2D/3D grid, in
+ * the order the reference's VTK writer visits it (z outermost, x innermost),
+ * -100 where the grid voxel is not tissue (GPU3D.cu:145-158 with stride 3,
+ * new_11.cu:164-175 with stride 1).  Sampled on the device.  out_host = NULL
+ * returns the count in *n. */
+int lqt_sim_sample_v(lqt_sim *s, int32_t stride, double *out_host, int64_t cap,
+                     int64_t *n);
+
+/* Legacy-VTK structured-points file of such samples, byte for byte the file
+ * of GPU3D.cu:123-163 / new_11.cu:142-180: header with DIMENSIONS
+ * nx/stride ny/stride nz/stride (integer division), values printed as a C++
+ * stream prints a double ("%g"), each followed by a space, a newline after
+ * every x row and after every z plane. */
+int lqt_io_write_vtk(const char *path, const double *samples_host, int32_t nx,
+                     int32_t ny, int32_t nz, int32_t stride);
+
+/* Rows of "%4.10f\t" values, each row ended by a newline: the .dat files of
+ * OneD.cc:402-415 (time, V of each cell), SingleCell.cc:113-139 (time, V,
+ * ICaL, IKs) and OneD_VW.cc (V of each cell).  append != 0 appends. */
+int lqt_io_write_dat(const char *path, int64_t nrows, int32_t ncols,
+                     const double *rows_host, int32_t append);
+
+/* Input files of the reference drivers.
+ * Geometry: one line per tissue voxel, "x y z fx fy fz code" (dim 3,
+ * GPU3D.cu:1276-1296,1424-1468) or "x y fx fy code" (dim 2,
+ * new_11.cu:1296-1302,1444-1478), into x-major grids of nx*ny*nz voxels (z
+ * fastest; nz = 1 in 2D): cell_type (codes 7-10, 17-20 -> LQT_EPI; 4-6,
+ * 14-16 -> LQT_MCELL; other codes -> LQT_ENDO; LQT_EMPTY where no line),
+ * code (the file's code after the edits, 0 elsewhere), fibre (3 floats per
+ * voxel; fz = 0 in 2D) and s2_mask.  case_edits = 1 applies the reference's
+ * case-study edits: 3D, RV M cells (codes 4-6) become code 2 if fy <= 4 else
+ * 7, LV M cells (14-16) outside 75 voxels of (597, 336, 336) become 12 (code
+ * 14) or 17, S2 box x in [300, 687), y in [120, 486), z in [420, 534)
+ * (GPU3D.cu:1437-1466); 2D, codes 3-6 become 2 (<= 4) or 7, LV M cells
+ * (13-16) outside x in [550, 689), y in [150, 487) become 12 or 17, S2 where
+ * x in [300, 400), y in [200, 350) and the original code is 11-13
+ * (new_11.cu:1452-1478).  Output arrays may be NULL.  Blank lines are
+ * skipped; a point outside the grid or a repeated point is an error. */
+typedef struct lqt_geom_file_spec {
+    int32_t dim;
+    int32_t nx, ny, nz;
+    int32_t case_edits;
+    int32_t reserved;          /* must be zero */
+} lqt_geom_file_spec;
+int lqt_io_read_geometry(const char *path, const lqt_geom_file_spec *spec,
+                         uint8_t *cell_type, uint8_t *code, float *fibre,
+                         uint8_t *s2_mask, int64_t *ntissue);
+/* Stimulation profile "x y z a b c onset tag" (GPU3D.cu:1694-1712): points
+ * that are tissue in cell_type get s1_mask = 1 and their onset (ms, read as
+ * float).  layer >= 0 (2D): only lines with z == layer, mapped to (x, y)
+ * (new_11.cu:1723-1741 uses layer 157).  Points off the grid or off tissue
+ * are skipped, as the reference skips them. */
+int lqt_io_read_stimulation(const char *path, int32_t nx, int32_t ny, int32_t nz,
+                            int32_t layer, const uint8_t *cell_type,
+                            uint8_t *s1_mask, float *onset, int64_t *npoints);
+
+/* Asynchronous VTK snapshots of a simulation: submit() samples V on the
+ * device and copies it into one of nbuf pinned buffers on the simulation's
+ * stream, then returns; a host thread writes the file once the copy is done
+ * (submit waits only when all buffers are in flight).  flush() waits for
+ * every pending file and reports the first write error.  The simulation must
+ * outlive the writer. */
+typedef struct lqt_vtk_writer lqt_vtk_writer;
+int lqt_vtk_writer_create(lqt_sim *s, int32_t stride, int32_t nbuf,
+                          lqt_vtk_writer **out);
+int lqt_vtk_writer_submit(lqt_vtk_writer *w, const char *path);
+int lqt_vtk_writer_flush(lqt_vtk_writer *w);
+void lqt_vtk_writer_destroy(lqt_vtk_writer *w);
 
 /* ======================================================================== *
  *  Learned surrogate network (no counterpart in the reference): MLP

@@ -12,7 +12,7 @@ from .cell import STATE_NAMES, TPORdCells, initial_state  # noqa: F401
 
 __all__ = ["TPORdCells", "Batch", "InstanceSpec", "OneDStrand", "oned_types", "initial_state", "model", "lib",
            "Model", "LqtError", "FP64", "MIXED", "LVEPI", "LVENDO", "EPI", "ENDO", "MCELL", "EMPTY", "STATE_NAMES"]
-from . import batch, geometry  # noqa: E402,F401
+from . import batch, geometry, protocols  # noqa: E402,F401
 from .sim import Sim  # noqa: E402,F401
 
 __all__ += ["Sim", "geometry"]

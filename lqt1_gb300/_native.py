@@ -34,7 +34,10 @@ class Instance(C.Structure):
     _fields_ = [("ncells", C.c_int32), ("n_stim", C.c_int32), ("model", C.c_int32), ("record", C.c_int32),
                 ("dx", C.c_double), ("bcl", C.c_double), ("s1_start", C.c_double), ("s1_duration", C.c_double),
                 ("s1_strength", C.c_double), ("s1_beats", C.c_int32), ("reserved0", C.c_int32),
-                ("t_stop", C.c_double), ("ecg_x0", C.c_double), ("act_threshold", C.c_double)]
+                ("t_stop", C.c_double), ("ecg_x0", C.c_double), ("act_threshold", C.c_double),
+                ("s2_base", C.c_double), ("s2_offset", C.c_double), ("s2_duration", C.c_double),
+                ("s2_strength", C.c_double), ("s2_cell0", C.c_int32), ("s2_ncells", C.c_int32),
+                ("track_vmax", C.c_int32), ("reserved1", C.c_int32)]
 
 
 class BatchParams(C.Structure):
@@ -98,6 +101,8 @@ def lib():
         "lqt_batch_run": ([P], I),
         "lqt_batch_get_detect": ([P, P, P, P, P, P], I),
         "lqt_batch_get_record": ([P, I32, P, P, P, I64, C.POINTER(I64)], I),
+        "lqt_batch_get_record_currents": ([P, I32, P, P, I64, C.POINTER(I64)], I),
+        "lqt_batch_get_vmax": ([P, P], I),
         "lqt_batch_get_state": ([P, P], I),
         "lqt_batch_set_state": ([P, P], I),
         "lqt_batch_last_run_ms": ([P], D),

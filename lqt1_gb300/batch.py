@@ -35,6 +35,15 @@ class InstanceSpec:
     ecg_x0: float = 35.0
     act_threshold: float = -30.0
     coeff: np.ndarray | None = None   # per-cell D, default 0.154
+    currents: bool = False            # with record: ICaL, IKs of the first cell too
+    # S2 (OneD_VW.cc): cells [s2_cell0, s2_cell0 + s2_ncells) at t - s2_base in [s2_offset, + s2_duration)
+    s2_base: float = 0.0
+    s2_offset: float = 0.0
+    s2_duration: float = 0.0
+    s2_strength: float = 0.0
+    s2_cell0: int = 0
+    s2_ncells: int = 0
+    track_vmax: bool = False          # maximum V of every cell from t - s2_base >= s2_offset
 
 
 class Batch:
@@ -50,7 +59,10 @@ class Batch:
             types.append(t)
             coeffs.append(np.full(len(t), 0.154) if s.coeff is None else np.asarray(s.coeff, np.float64))
             a = arr[i]
-            a.ncells, a.n_stim, a.model, a.record = len(t), s.n_stim, s.model, int(s.record)
+            a.ncells, a.n_stim, a.model = len(t), s.n_stim, s.model
+            a.record = (3 if s.currents else 1) if s.record else 0
+            a.s2_base, a.s2_offset, a.s2_duration, a.s2_strength = s.s2_base, s.s2_offset, s.s2_duration, s.s2_strength
+            a.s2_cell0, a.s2_ncells, a.track_vmax = s.s2_cell0, s.s2_ncells, int(s.track_vmax)
             a.dx, a.bcl, a.s1_start, a.s1_duration, a.s1_strength = s.dx, s.bcl, s.s1_start, s.s1_duration, s.s1_strength
             a.s1_beats, a.t_stop, a.ecg_x0, a.act_threshold = s.s1_beats, s.t_stop, s.ecg_x0, s.act_threshold
         self.types = np.concatenate(types)
@@ -104,12 +116,24 @@ class Batch:
         N.check(N.lib().lqt_batch_get_record(self._h, i, None, None, None, 0, C.byref(nrec)), "lqt_batch_get_record")
         m = nrec.value
         n = len(self.instances[i].types)
-        v = np.zeros((m, n), np.float32)
+        v = np.zeros((m, n))
         t = np.zeros(m)
         ecg = np.zeros(m)
         N.check(N.lib().lqt_batch_get_record(self._h, i, _p(v), _p(t), _p(ecg), m, C.byref(nrec)),
                 "lqt_batch_get_record")
-        return dict(v=v, t=t, ecg=ecg)
+        out = dict(v=v, t=t, ecg=ecg)
+        if self.instances[i].currents:
+            ical, iks = np.zeros(m), np.zeros(m)
+            N.check(N.lib().lqt_batch_get_record_currents(self._h, i, _p(ical), _p(iks), m, C.byref(nrec)),
+                    "lqt_batch_get_record_currents")
+            out.update(ical=ical, iks=iks)
+        return out
+
+    def vmax(self):
+        """Per cell (input order): maximum V of the track_vmax watch."""
+        out = np.zeros(self.ncells, np.float32)
+        N.check(N.lib().lqt_batch_get_vmax(self._h, _p(out)), "lqt_batch_get_vmax")
+        return out
 
     def get_state(self):
         s = np.zeros((self.ncells, N.NSTATE))

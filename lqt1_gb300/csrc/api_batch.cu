@@ -49,8 +49,9 @@ struct lqt_batch {
     ModelK *models = nullptr;
     int *queue = nullptr;
     unsigned long long *nbad = nullptr;
-    float *rec_v = nullptr;
+    double *rec_v = nullptr, *rec_cur = nullptr;
     double *rec_t = nullptr, *ecg = nullptr;
+    float *vmax = nullptr;
     float *det_t_act = nullptr, *det_apd90 = nullptr, *det_dvdt = nullptr;
     uint8_t *det_ead = nullptr;
     int32_t *det_beats = nullptr;
@@ -86,6 +87,8 @@ struct lqt_batch {
         b.rec_cap = rec_cap;
         b.rec_width = rec_width;
         b.rec_v = rec_v;
+        b.rec_cur = rec_cur;
+        b.vmax = vmax;
         b.rec_t = rec_t;
         b.ecg = ecg;
         b.det_t_act = det_t_act;
@@ -266,9 +269,12 @@ int lqt_batch_create(const lqt_batch_params *params, int32_t ninst, const lqt_in
         const lqt_instance &q = inst[i];
         if (q.ncells < 1 || q.ncells > 512 || q.model < 0 || q.model >= nmodels || q.n_stim < 0 ||
             !(q.t_stop >= 0) || !std::isfinite(q.t_stop) || !(q.bcl > 0) || q.s1_duration < 0 || q.s1_beats < 0 ||
-            (q.ncells > 1 && !(q.dx > 0)) || q.t_stop > 1e7)
+            (q.ncells > 1 && !(q.dx > 0)) || q.t_stop > 1e7 || q.s2_ncells < 0 || q.s2_cell0 < 0 ||
+            (q.s2_ncells > 0 && q.s2_cell0 + q.s2_ncells > q.ncells) || q.s2_duration < 0 || q.record < 0 ||
+            q.record > 3 || q.reserved0 != 0 || q.reserved1 != 0)
             return fail(LQT_ERR_INVALID, "lqt_batch_create: instance " + std::to_string(i) +
-                                             " invalid (ncells 1..512, model index, bcl > 0, t_stop, dx > 0)");
+                                             " invalid (ncells 1..512, model index, bcl > 0, t_stop, dx > 0, "
+                                             "S2 cells inside the instance, record 0..3, reserved 0)");
         max_strand = std::max(max_strand, (int)q.ncells);
         ncells += q.ncells;
         t_max = std::max(t_max, q.t_stop);
@@ -337,6 +343,7 @@ int lqt_batch_create(const lqt_batch_params *params, int32_t ninst, const lqt_in
     b->rec_slot.assign(ninst, -1);
     int32_t nrec_slots = 0;
     int64_t next_cell = 0;
+    bool any_cur = false, any_vmax = false;
     for (int oi : order) {
         const lqt_instance &q = inst[oi];
         Seg sg{};
@@ -353,6 +360,29 @@ int lqt_batch_create(const lqt_batch_params *params, int32_t ninst, const lqt_in
         sg.ecg_x0 = q.ecg_x0;
         sg.act_thr = (float)q.act_threshold;
         sg.rec_slot = -1;
+        sg.rec_cur = (q.record & 2) ? 1 : 0;
+        any_cur |= sg.rec_cur != 0;
+        // S2 and the maximum-V watch on the same floating time axis as the
+        // reference: t - base >= offset (OneD_VW.cc:273-275,340)
+        sg.s2_on = sg.s2_off = sg.vmax_from = INT64_MAX;
+        sg.s2_c0 = q.s2_cell0;
+        sg.s2_n = q.s2_ncells;
+        sg.s2_stim = q.s2_strength;
+        if (q.s2_ncells > 0 || q.track_vmax) {
+            for (int64_t k = 0; k < sg.nsteps; ++k) {
+                const double rel = times[k] - q.s2_base;
+                if (rel >= q.s2_offset) {
+                    if (sg.vmax_from == INT64_MAX) sg.vmax_from = k;
+                    if (rel < q.s2_offset + q.s2_duration) {
+                        if (sg.s2_on == INT64_MAX) sg.s2_on = k;
+                        sg.s2_off = k + 1;
+                    }
+                }
+            }
+            if (q.s2_ncells <= 0) sg.s2_on = sg.s2_off = INT64_MAX;
+            if (!q.track_vmax) sg.vmax_from = INT64_MAX;
+        }
+        any_vmax |= q.track_vmax != 0;
         if (q.record) {
             sg.rec_slot = nrec_slots++;
             b->rec_slot[oi] = sg.rec_slot;
@@ -414,10 +444,12 @@ int lqt_batch_create(const lqt_batch_params *params, int32_t ninst, const lqt_in
     rc |= b->mem.alloc((void **)&b->queue, 16);
     rc |= b->mem.alloc((void **)&b->nbad, 16);
     if (nrec_slots) {
-        rc |= b->mem.alloc((void **)&b->rec_v, (size_t)nrec_slots * b->rec_cap * b->rec_width * 4);
+        rc |= b->mem.alloc((void **)&b->rec_v, (size_t)nrec_slots * b->rec_cap * b->rec_width * 8);
+        if (any_cur) rc |= b->mem.alloc((void **)&b->rec_cur, (size_t)nrec_slots * b->rec_cap * 2 * 8);
         rc |= b->mem.alloc((void **)&b->rec_t, (size_t)nrec_slots * b->rec_cap * 8);
         rc |= b->mem.alloc((void **)&b->ecg, (size_t)nrec_slots * b->rec_cap * 8);
     }
+    if (any_vmax) rc |= b->mem.alloc((void **)&b->vmax, ncells * 4);
     if (nb > 0) {
         rc |= b->mem.alloc((void **)&b->det_t_act, ncells * nb * 4);
         rc |= b->mem.alloc((void **)&b->det_apd90, ncells * nb * 4);
@@ -548,7 +580,7 @@ int lqt_batch_get_detect(lqt_batch *b, float *t_act, float *apd90, float *dvdt_m
     return LQT_OK;
 }
 
-int lqt_batch_get_record(lqt_batch *b, int32_t i, float *v, double *t, double *ecg, int64_t cap, int64_t *nrec)
+int lqt_batch_get_record(lqt_batch *b, int32_t i, double *v, double *t, double *ecg, int64_t cap, int64_t *nrec)
 {
     if (!b || i < 0 || i >= b->ninst) return fail(LQT_ERR_INVALID, "lqt_batch_get_record: bad handle or instance");
     const int slot = b->rec_slot[i];
@@ -559,13 +591,44 @@ int lqt_batch_get_record(lqt_batch *b, int32_t i, float *v, double *t, double *e
     const int64_t m = std::min(nr, cap);
     const int n = b->inst[i].ncells;
     if (v && m > 0) {
-        std::vector<float> buf((size_t)(m * b->rec_width));
-        CK(cudaMemcpy(buf.data(), b->rec_v + (int64_t)slot * b->rec_cap * b->rec_width, m * b->rec_width * 4,
+        std::vector<double> buf((size_t)(m * b->rec_width));
+        CK(cudaMemcpy(buf.data(), b->rec_v + (int64_t)slot * b->rec_cap * b->rec_width, m * b->rec_width * 8,
                       cudaMemcpyDeviceToHost));
-        for (int64_t r = 0; r < m; ++r) std::memcpy(v + r * n, &buf[r * b->rec_width], n * 4);
+        for (int64_t r = 0; r < m; ++r) std::memcpy(v + r * n, &buf[r * b->rec_width], n * 8);
     }
     if (t && m > 0) CK(cudaMemcpy(t, b->rec_t + (int64_t)slot * b->rec_cap, m * 8, cudaMemcpyDeviceToHost));
     if (ecg && m > 0) CK(cudaMemcpy(ecg, b->ecg + (int64_t)slot * b->rec_cap, m * 8, cudaMemcpyDeviceToHost));
+    return LQT_OK;
+}
+
+int lqt_batch_get_record_currents(lqt_batch *b, int32_t i, double *ical, double *iks, int64_t cap, int64_t *nrec)
+{
+    if (!b || i < 0 || i >= b->ninst) return fail(LQT_ERR_INVALID, "lqt_batch_get_record_currents: bad handle or instance");
+    const int slot = b->rec_slot[i];
+    if (slot < 0 || !(b->inst[i].record & 2) || !b->rec_cur)
+        return fail(LQT_ERR_STATE, "lqt_batch_get_record_currents: instance was not recorded with currents");
+    const int64_t ns = b->inst_nsteps[i];
+    const int64_t nr = std::min<int64_t>((ns + b->p.rec_every - 1) / b->p.rec_every, b->rec_cap);
+    if (nrec) *nrec = nr;
+    const int64_t m = std::min(nr, cap);
+    if (m > 0 && (ical || iks)) {
+        std::vector<double> buf((size_t)m * 2);
+        CK(cudaMemcpy(buf.data(), b->rec_cur + (int64_t)slot * b->rec_cap * 2, m * 16, cudaMemcpyDeviceToHost));
+        for (int64_t r = 0; r < m; ++r) {
+            if (ical) ical[r] = buf[2 * r];
+            if (iks) iks[r] = buf[2 * r + 1];
+        }
+    }
+    return LQT_OK;
+}
+
+int lqt_batch_get_vmax(lqt_batch *b, float *vmax_host)
+{
+    if (!b || !vmax_host) return fail(LQT_ERR_INVALID, "lqt_batch_get_vmax: NULL");
+    if (!b->vmax) return fail(LQT_ERR_STATE, "lqt_batch_get_vmax: no instance has track_vmax set");
+    std::vector<float> buf((size_t)b->ncells);
+    CK(cudaMemcpy(buf.data(), b->vmax, b->ncells * 4, cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < b->ncells; ++i) vmax_host[b->perm[i]] = buf[i];
     return LQT_OK;
 }
 

@@ -11,9 +11,13 @@
 
 #include <algorithm>
 #include <cmath>
+#include <condition_variable>
 #include <cstdio>
 #include <cstring>
+#include <deque>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "api_common.h"
@@ -85,6 +89,10 @@ struct lqt_sim {
     unsigned long long *sur_stats = nullptr;
     int *sur_err = nullptr;
     int64_t sur_launches = 0;
+    // output sampling: tissue mask of the dense grid, lattice buffer
+    uint8_t *tmask = nullptr;
+    double *samp = nullptr;
+    int64_t samp_cap = 0;
     // graph
     cudaGraphExec_t graph = nullptr;
     int graph_cur = -1;
@@ -356,6 +364,32 @@ int autotune(lqt_sim *s, int per, int64_t *consumed)
     s->tuned = true;
     s->graph_valid = false;
     return rc;
+}
+
+// 1 where a dense-grid voxel is tissue (uploaded on first use).
+int ensure_tmask(lqt_sim *s)
+{
+    if (s->tmask) return LQT_OK;
+    std::vector<uint8_t> m((size_t)s->ngrid, 0);
+    for (int64_t k = 0; k < s->ntissue; ++k) m[(size_t)s->tm.cells[k]] = 1;
+    if (s->mem.alloc((void **)&s->tmask, s->ngrid)) return LQT_ERR_NOMEM;
+    CK(cudaMemcpy(s->tmask, m.data(), s->ngrid, cudaMemcpyHostToDevice));
+    return LQT_OK;
+}
+
+// The VTK lattice of the current V into dev_out (device), on the simulation's stream.
+int sample_launch(lqt_sim *s, int32_t stride, double *dev_out)
+{
+    int rc = ensure_tmask(s);
+    if (rc) return rc;
+    const int64_t sx = (int64_t)s->ny * s->nz, sy = s->dim == 2 ? 1 : s->nz;
+    if (s->fp64())
+        CK(launch_sample_v<double>((const double *)s->vg[s->cur], s->tmask, s->nx, s->ny, s->nz, stride, sx, sy,
+                                   dev_out, s->stream));
+    else
+        CK(launch_sample_v<float>((const float *)s->vg[s->cur], s->tmask, s->nx, s->ny, s->nz, stride, sx, sy,
+                                  dev_out, s->stream));
+    return LQT_OK;
 }
 
 int build_graph(lqt_sim *s)
@@ -937,6 +971,30 @@ int lqt_sim_check(lqt_sim *s, int64_t *n_bad)
     return v ? LQT_ERR_NUMERIC : LQT_OK;
 }
 
+int lqt_sim_sample_v(lqt_sim *s, int32_t stride, double *out_host, int64_t cap, int64_t *n)
+{
+    if (!s || !n || stride < 1) return fail(LQT_ERR_INVALID, "lqt_sim_sample_v: NULL or stride < 1");
+    if (s->dim < 2) return fail(LQT_ERR_INVALID, "lqt_sim_sample_v: 2D and 3D grids only");
+    const int64_t cnt = vtk_samples(s->nx, s->ny, s->nz, stride);
+    *n = cnt;
+    if (!out_host) return LQT_OK;
+    if (cap < cnt) return fail(LQT_ERR_INVALID, "lqt_sim_sample_v: cap below the sample count");
+    if (cnt > s->samp_cap) {
+        if (s->samp) {
+            cudaFree(s->samp);
+            s->mem.ptrs.erase(std::remove(s->mem.ptrs.begin(), s->mem.ptrs.end(), (void *)s->samp), s->mem.ptrs.end());
+            s->samp = nullptr;
+        }
+        if (s->mem.alloc((void **)&s->samp, cnt * 8)) return LQT_ERR_NOMEM;
+        s->samp_cap = cnt;
+    }
+    int rc = sample_launch(s, stride, s->samp);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(out_host, s->samp, cnt * 8, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return LQT_OK;
+}
+
 int lqt_sim_set_surrogate(lqt_sim *s, lqt_mlp *m, const lqt_sur_config *cfg)
 {
     if (!s) return fail(LQT_ERR_INVALID, "lqt_sim_set_surrogate: NULL handle");
@@ -1048,6 +1106,160 @@ int lqt_sim_restore(lqt_sim *s, const char *path)
     s->time = time;
     s->graph_valid = false;
     return lqt_sim_set_state(s, st.data());
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Asynchronous VTK writer: the lattice is sampled on the device and copied
+// into a pinned buffer on the simulation's stream; a host thread formats and
+// writes the file once that copy has completed, while the simulation steps on.
+struct lqt_vtk_writer {
+    lqt_sim *s = nullptr;
+    int32_t stride = 3;
+    int64_t n = 0;
+    std::vector<double *> dbuf, hbuf;
+    std::vector<cudaEvent_t> ev;
+    std::vector<bool> busy;
+    std::deque<std::pair<int, std::string>> jobs;
+    std::mutex mu;
+    std::condition_variable cv;
+    bool stop = false;
+    int err = LQT_OK;
+    std::string errmsg;
+    std::thread th;
+
+    void run()
+    {
+        for (;;) {
+            std::pair<int, std::string> job;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                cv.wait(lk, [&] { return stop || !jobs.empty(); });
+                if (jobs.empty()) return;
+                job = jobs.front();
+                jobs.pop_front();
+            }
+            int rc = LQT_OK;
+            std::string msg;
+            if (cudaEventSynchronize(ev[job.first]) != cudaSuccess) {
+                rc = LQT_ERR_CUDA;
+                msg = "lqt_vtk_writer: device copy failed";
+            } else {
+                rc = write_vtk_file(job.second.c_str(), hbuf[job.first], s->nx, s->ny, s->nz, stride);
+                if (rc) msg = g_err;
+            }
+            std::lock_guard<std::mutex> lk(mu);
+            busy[job.first] = false;
+            if (rc && err == LQT_OK) {
+                err = rc;
+                errmsg = msg;
+            }
+            cv.notify_all();
+        }
+    }
+    ~lqt_vtk_writer()
+    {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            stop = true;
+        }
+        cv.notify_all();
+        if (th.joinable()) th.join();
+        for (auto p : dbuf) if (p) cudaFree(p);
+        for (auto p : hbuf) if (p) cudaFreeHost(p);
+        for (auto e : ev) if (e) cudaEventDestroy(e);
+    }
+};
+
+extern "C" {
+
+int lqt_vtk_writer_create(lqt_sim *s, int32_t stride, int32_t nbuf, lqt_vtk_writer **out)
+{
+    if (!out) return fail(LQT_ERR_INVALID, "lqt_vtk_writer_create: out is NULL");
+    *out = nullptr;
+    if (!s || stride < 1 || nbuf < 1 || nbuf > 16)
+        return fail(LQT_ERR_INVALID, "lqt_vtk_writer_create: NULL, stride < 1 or nbuf outside 1..16");
+    if (s->dim < 2) return fail(LQT_ERR_INVALID, "lqt_vtk_writer_create: 2D and 3D grids only");
+    auto *w = new lqt_vtk_writer();
+    w->s = s;
+    w->stride = stride;
+    w->n = vtk_samples(s->nx, s->ny, s->nz, stride);
+    w->dbuf.assign(nbuf, nullptr);
+    w->hbuf.assign(nbuf, nullptr);
+    w->ev.assign(nbuf, nullptr);
+    w->busy.assign(nbuf, false);
+    for (int i = 0; i < nbuf; ++i) {
+        if (cudaMalloc((void **)&w->dbuf[i], w->n * 8) != cudaSuccess ||
+            cudaHostAlloc((void **)&w->hbuf[i], w->n * 8, cudaHostAllocDefault) != cudaSuccess ||
+            cudaEventCreateWithFlags(&w->ev[i], cudaEventDisableTiming) != cudaSuccess) {
+            delete w;
+            return fail(LQT_ERR_NOMEM, "lqt_vtk_writer_create: buffer allocation failed");
+        }
+    }
+    w->th = std::thread([w] { w->run(); });
+    *out = w;
+    return LQT_OK;
+}
+
+int lqt_vtk_writer_submit(lqt_vtk_writer *w, const char *path)
+{
+    if (!w || !path) return fail(LQT_ERR_INVALID, "lqt_vtk_writer_submit: NULL");
+    int idx = -1;
+    {
+        std::unique_lock<std::mutex> lk(w->mu);
+        w->cv.wait(lk, [&] {
+            if (w->err) return true;
+            for (size_t i = 0; i < w->busy.size(); ++i)
+                if (!w->busy[i]) return true;
+            return false;
+        });
+        if (w->err) return fail(w->err, w->errmsg);
+        for (size_t i = 0; i < w->busy.size(); ++i)
+            if (!w->busy[i]) {
+                idx = (int)i;
+                break;
+            }
+        w->busy[idx] = true;
+    }
+    lqt_sim *s = w->s;
+    int rc = sample_launch(s, w->stride, w->dbuf[idx]);
+    cudaError_t e = rc ? cudaSuccess : cudaMemcpyAsync(w->hbuf[idx], w->dbuf[idx], w->n * 8, cudaMemcpyDeviceToHost,
+                                                       s->stream);
+    if (!rc && e == cudaSuccess) e = cudaEventRecord(w->ev[idx], s->stream);
+    std::lock_guard<std::mutex> lk(w->mu);
+    if (rc || e != cudaSuccess) {
+        w->busy[idx] = false;
+        return rc ? rc : fail(LQT_ERR_CUDA, std::string("lqt_vtk_writer_submit: ") + cudaGetErrorString(e));
+    }
+    w->jobs.emplace_back(idx, std::string(path));
+    w->cv.notify_all();
+    return LQT_OK;
+}
+
+int lqt_vtk_writer_flush(lqt_vtk_writer *w)
+{
+    if (!w) return fail(LQT_ERR_INVALID, "lqt_vtk_writer_flush: NULL");
+    std::unique_lock<std::mutex> lk(w->mu);
+    w->cv.wait(lk, [&] {
+        if (!w->jobs.empty()) return false;
+        for (bool b : w->busy)
+            if (b) return false;
+        return true;
+    });
+    if (w->err) {
+        const int rc = w->err;
+        w->err = LQT_OK;
+        return fail(rc, w->errmsg);
+    }
+    return LQT_OK;
+}
+
+void lqt_vtk_writer_destroy(lqt_vtk_writer *w)
+{
+    if (!w) return;
+    lqt_vtk_writer_flush(w);
+    delete w;
 }
 
 }  // extern "C"

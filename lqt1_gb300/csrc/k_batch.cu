@@ -96,6 +96,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_batch(BatchDev<R> b, StepT<R> k)
         }
         DetState det{};
         det.phase = kDetIdle;
+        R vmax = (R)-100;    // the starting value of maxEndo / maxEpi, OneD_VW.cc:246-247
         float t_act = -1.f;
         int beat = 0;        // cycles opened so far
         int nact = 0;        // activations recorded
@@ -164,8 +165,12 @@ __global__ void __launch_bounds__(MAXT, MINB) k_batch(BatchDev<R> b, StepT<R> k)
                     }
                 }
                 if (st == w_on) opened = true;
-                const bool on = st >= w_on && st < w_off && li < seg.n_stim;
-                const R ist = on ? stim : (R)0;
+                const bool s1_open = st >= w_on && st < w_off;
+                const bool on = s1_open && li < seg.n_stim;
+                // S2 only while no S1 window is open (OneD_VW.cc:265-279)
+                const bool on2 = !s1_open && st >= seg.s2_on && st < seg.s2_off && li >= seg.s2_c0 &&
+                                 li < seg.s2_c0 + seg.s2_n;
+                const R ist = on ? stim : (on2 ? (R)seg.s2_stim : (R)0);
                 if (opened && b.det_t_act) {
                     det_open_cycle(det, (float)vo);
                     ++beat;
@@ -173,6 +178,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_batch(BatchDev<R> b, StepT<R> k)
                 StepOut<R> o{};
                 tpord_step<R>(c, ct, m, k, ist, dvgap, &o);
                 vbuf[cur ^ 1][t] = c.v;
+                if (st >= seg.vmax_from && c.v >= vmax) vmax = c.v;
 
                 if (b.det_t_act && det.phase != kDetIdle) {
                     DetEvent ev;
@@ -192,8 +198,13 @@ __global__ void __launch_bounds__(MAXT, MINB) k_batch(BatchDev<R> b, StepT<R> k)
                 if (seg.rec_slot >= 0 && (st % b.rec_every) == 0) {
                     const int64_t slot = st / b.rec_every;
                     if (slot < b.rec_cap) {
-                        b.rec_v[((int64_t)seg.rec_slot * b.rec_cap + slot) * b.rec_width + li] = (float)c.v;
+                        b.rec_v[((int64_t)seg.rec_slot * b.rec_cap + slot) * b.rec_width + li] = (double)c.v;
                         if (li == 0) b.rec_t[(int64_t)seg.rec_slot * b.rec_cap + slot] = time;
+                        if (li == 0 && seg.rec_cur) {
+                            double *rc = b.rec_cur + ((int64_t)seg.rec_slot * b.rec_cap + slot) * 2;
+                            rc[0] = (double)o.ical;
+                            rc[1] = (double)o.iks;
+                        }
                     }
                 }
                 if (!(c.v == c.v) || c.v < (R)b.vmin_ok || c.v > (R)b.vmax_ok) atomicAdd(b.nbad, 1ull);
@@ -230,6 +241,7 @@ __global__ void __launch_bounds__(MAXT, MINB) k_batch(BatchDev<R> b, StepT<R> k)
             store_cell(c, b.s, cell);
             b.s.v[cell] = c.v;
             if (b.det_beats) b.det_beats[cell] = nact;
+            if (b.vmax) b.vmax[cell] = (float)vmax;
         }
     }
 }

@@ -105,4 +105,33 @@ template cudaError_t launch_gather_v<double, double>(const double *, const int32
 template cudaError_t launch_scatter_v<float>(const float *, const int32_t *, float *, int64_t, cudaStream_t);
 template cudaError_t launch_scatter_v<double>(const double *, const int32_t *, double *, int64_t, cudaStream_t);
 
+// V on the lattice of every `stride`-th voxel per axis, in the order the
+// reference's VTK writer visits it (z outermost, x innermost); -100 where the
+// grid voxel is not tissue (GPU3D.cu:145-158, new_11.cu:164-175).
+template <typename R>
+__global__ void k_sample_v(const R *__restrict__ vg, const uint8_t *__restrict__ tissue, int32_t nx, int32_t ny,
+                           int32_t nz, int32_t stride, int64_t sx, int64_t sy, double *__restrict__ out)
+{
+    const int64_t cx = (nx + stride - 1) / stride, cy = (ny + stride - 1) / stride, cz = (nz + stride - 1) / stride;
+    const int64_t n = cx * cy * cz;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t xi = i % cx, r = i / cx, yi = r % cy, zi = r / cy;
+        const int64_t g = xi * stride * sx + yi * stride * sy + zi * stride;
+        out[i] = tissue[g] ? (double)vg[g] : -100.0;
+    }
+}
+template <typename R>
+cudaError_t launch_sample_v(const R *vg, const uint8_t *tissue, int32_t nx, int32_t ny, int32_t nz, int32_t stride,
+                            int64_t sx, int64_t sy, double *out, cudaStream_t st)
+{
+    const int64_t n = ((nx + stride - 1) / stride) * (int64_t)((ny + stride - 1) / stride) * ((nz + stride - 1) / stride);
+    if (n <= 0) return cudaSuccess;
+    k_sample_v<R><<<grid_for(n, 256), 256, 0, st>>>(vg, tissue, nx, ny, nz, stride, sx, sy, out);
+    return cudaGetLastError();
+}
+template cudaError_t launch_sample_v<float>(const float *, const uint8_t *, int32_t, int32_t, int32_t, int32_t, int64_t,
+                                            int64_t, double *, cudaStream_t);
+template cudaError_t launch_sample_v<double>(const double *, const uint8_t *, int32_t, int32_t, int32_t, int32_t,
+                                             int64_t, int64_t, double *, cudaStream_t);
+
 }  // namespace lqt

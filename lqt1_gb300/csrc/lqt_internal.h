@@ -37,7 +37,11 @@ struct Seg {
     double stim;          // pA/pF
     double ecg_x0;        // electrode position, mm (plot1DECG_compare.py:83)
     float act_thr;        // mV
-    float pad;
+    int32_t rec_cur;      // 1: ICaL, IKs of the first cell recorded too
+    int64_t s2_on, s2_off;  // S2 step range (OneD_VW.cc:273-279)
+    int32_t s2_c0, s2_n;    // cells [s2_c0, s2_c0 + s2_n) receive S2
+    double s2_stim;         // pA/pF
+    int64_t vmax_from;      // first step of the maximum-V watch, INT64_MAX = off
 };
 
 // A CTA's unit of work: contiguous cells [cell0, cell0 + ncells).
@@ -67,7 +71,9 @@ template <typename R> struct BatchDev {
     // recording
     int64_t rec_every, rec_cap;
     int32_t rec_width;               // max cells of a recorded segment
-    float *rec_v;                    // [slot][rec_cap][rec_width]
+    double *rec_v;                   // [slot][rec_cap][rec_width]
+    double *rec_cur;                 // [slot][rec_cap][2]: ICaL, IKs of the first cell
+    float *vmax;                     // per cell: maximum V since vmax_from, or null
     double *rec_t;                   // [slot][rec_cap]
     double *ecg;                     // [slot][rec_cap]
     // detectors ([cell][max_beats]), or null
@@ -95,4 +101,9 @@ namespace lqt {
 template <typename R, typename T>
 cudaError_t launch_gather_v(const R *vg, const int32_t *gidx, T *out, int64_t n, cudaStream_t st);
 template <typename R> cudaError_t launch_scatter_v(const R *v, const int32_t *gidx, R *vg, int64_t n, cudaStream_t st);
+template <typename R>
+cudaError_t launch_sample_v(const R *vg, const uint8_t *tissue, int32_t nx, int32_t ny, int32_t nz, int32_t stride,
+                            int64_t sx, int64_t sy, double *out, cudaStream_t st);
+int write_vtk_file(const char *path, const double *samples, int32_t nx, int32_t ny, int32_t nz, int32_t stride);
+int64_t vtk_samples(int32_t nx, int32_t ny, int32_t nz, int32_t stride);
 }  // namespace lqt

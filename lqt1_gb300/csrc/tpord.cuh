@@ -127,6 +127,7 @@ template <typename R> struct CellState {
 
 template <typename R> struct StepOut {
     R dvdt;        // -(Iion + Ist) (TPORd.cc:928)
+    R ical, iks;   // ICaL and IKs of the step (TPORd::getICaL / getIKs, SingleCell.cc:134-135)
 };
 
 // One TPORd update.  ctype: 2 = EPI, 4 = MCELL, other = endocardial
@@ -446,7 +447,11 @@ __device__ __forceinline__ void tpord_step(CellState<R> &c, int ctype, const Mod
     const R Iion = INa + INaL + Ito + ICaL + ICaNa + ICaK + IKr + IKs + IK1 + INaCa + INaK + INab + IKb + IpCa + ICab;
     const R dV_dt = (R)-1 * (Iion + Ist);
     c.v = v + (dV_dt + dVgap_dt) * dt;
-    if (out) out->dvdt = dV_dt;
+    if (out) {
+        out->dvdt = dV_dt;
+        out->ical = ICaL;
+        out->iks = IKs;
+    }
 
     // CaMK and fluxes, TPORd.cc:939-995
     c.CaMKt += dt * ((R)0.05 * CaMKb * (CaMKb + c.CaMKt) - (R)0.00068 * c.CaMKt);

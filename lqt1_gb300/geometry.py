@@ -9,6 +9,7 @@ same layout (x-major, z fastest; empty voxels = LQT_EMPTY).
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass
 
 import numpy as np
@@ -98,3 +99,57 @@ def mirror_map(types: np.ndarray):
     src = np.zeros(n.value, np.int64)
     N.check(L.lqt_geom_mirror_map(*shp, _p(g), _p(tissue_of), _p(dst), _p(src), C.byref(n)), "lqt_geom_mirror_map")
     return tissue_of, dst, src
+
+
+# ---- the reference drivers' input files -------------------------------------
+class GeomFileSpec(C.Structure):
+    _fields_ = [("dim", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+                ("case_edits", C.c_int32), ("reserved", C.c_int32)]
+
+
+@dataclass
+class LoadedGeometry:
+    types: np.ndarray      # cell types per grid voxel (LQT_EMPTY off tissue)
+    code: np.ndarray       # the file's code after the case edits (0 off tissue)
+    fibre: np.ndarray      # fibre vector per voxel
+    s2_mask: np.ndarray
+    ntissue: int
+
+
+def load_geometry(path: str, shape, case_edits: bool = True, fibre: bool = True) -> LoadedGeometry:
+    """A geometry text file of the reference (3D: "x y z fx fy fz code",
+    GPU3D.cu:1276-1468; 2D: "x y fx fy code", new_11.cu:1296-1478) on a grid
+    of `shape` (nx, ny, nz) or (nx, ny)."""
+    L = N.lib()
+    L.lqt_io_read_geometry.argtypes = [C.c_char_p, C.POINTER(GeomFileSpec), C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.POINTER(C.c_int64)]
+    dim = len(shape)
+    nx, ny = shape[0], shape[1]
+    nz = shape[2] if dim == 3 else 1
+    sp = GeomFileSpec(dim, nx, ny, nz, int(case_edits), 0)
+    g = (nx, ny, nz) if dim == 3 else (nx, ny)
+    types = np.empty(g, np.uint8)
+    code = np.empty(g, np.uint8)
+    fib = np.empty(g + (3,), np.float32) if fibre else None
+    s2 = np.empty(g, np.uint8)
+    n = C.c_int64()
+    N.check(L.lqt_io_read_geometry(os.fsencode(path), C.byref(sp), _p(types), _p(code), _p(fib), _p(s2), C.byref(n)),
+            "lqt_io_read_geometry")
+    return LoadedGeometry(types, code, fib, s2, int(n.value))
+
+
+def load_stimulation(path: str, types: np.ndarray, layer: int = -1):
+    """Stimulation profile "x y z a b c onset tag" (GPU3D.cu:1694-1712;
+    layer >= 0 keeps one z layer for a 2D grid, new_11.cu:1723-1741).
+    Returns (s1_mask, onset ms) on the grid of `types`."""
+    L = N.lib()
+    L.lqt_io_read_stimulation.argtypes = [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
+                                          C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]
+    t = np.ascontiguousarray(types, np.uint8)
+    shp = t.shape + (1,) * (3 - t.ndim)
+    mask = np.empty(t.shape, np.uint8)
+    onset = np.empty(t.shape, np.float32)
+    n = C.c_int64()
+    N.check(L.lqt_io_read_stimulation(os.fsencode(path), shp[0], shp[1], shp[2], layer, _p(t), _p(mask), _p(onset),
+                                      C.byref(n)), "lqt_io_read_stimulation")
+    return mask, onset

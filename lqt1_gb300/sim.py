@@ -8,6 +8,7 @@ check and checkpoints.
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -121,6 +122,21 @@ class Sim:
         N.check(L.lqt_sim_profile(self._h, int(nsteps), C.byref(a), C.byref(b), C.byref(c)), "lqt_sim_profile")
         return a.value, b.value, c.value
 
+    # ---- output files ----------------------------------------------------------------
+    def sample_v(self, stride: int = 3) -> np.ndarray:
+        """V on the VTK lattice (every `stride`-th voxel per axis, z outermost,
+        x innermost, -100 off tissue), sampled on the device."""
+        L = N.lib()
+        L.lqt_sim_sample_v.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]
+        n = C.c_int64()
+        N.check(L.lqt_sim_sample_v(self._h, stride, None, 0, C.byref(n)), "lqt_sim_sample_v")
+        out = np.zeros(n.value)
+        N.check(L.lqt_sim_sample_v(self._h, stride, _p(out), n.value, C.byref(n)), "lqt_sim_sample_v")
+        return out
+
+    def vtk_writer(self, stride: int = 3, nbuf: int = 2) -> "VtkWriter":
+        return VtkWriter(self, stride, nbuf)
+
     # ---- learned surrogate ---------------------------------------------------------
     def set_surrogate(self, mlp=None, *, dvdt_max: float = 1.0, kappa: float = 1.5, vstep_max: float = 0.3,
                       use_net: bool = True):
@@ -191,3 +207,39 @@ class Sim:
 
     def restore(self, path: str):
         N.check(N.lib().lqt_sim_restore(self._h, path.encode()), "lqt_sim_restore")
+
+
+class VtkWriter:
+    """Asynchronous VTK snapshots of a Sim (lqt_vtk_writer_*): submit(path)
+    samples V on the device and returns; a host thread writes the file."""
+
+    def __init__(self, sim: Sim, stride: int = 3, nbuf: int = 2):
+        L = N.lib()
+        L.lqt_vtk_writer_create.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]
+        L.lqt_vtk_writer_submit.argtypes = [C.c_void_p, C.c_char_p]
+        L.lqt_vtk_writer_flush.argtypes = [C.c_void_p]
+        L.lqt_vtk_writer_destroy.argtypes = [C.c_void_p]
+        L.lqt_vtk_writer_destroy.restype = None
+        h = C.c_void_p()
+        N.check(L.lqt_vtk_writer_create(sim._h, stride, nbuf, C.byref(h)), "lqt_vtk_writer_create")
+        self._h, self._sim, self.L = h, sim, L
+
+    def submit(self, path: str):
+        N.check(self.L.lqt_vtk_writer_submit(self._h, os.fsencode(path)), "lqt_vtk_writer_submit")
+
+    def flush(self):
+        N.check(self.L.lqt_vtk_writer_flush(self._h), "lqt_vtk_writer_flush")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.L.lqt_vtk_writer_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.flush()
+        self.close()

@@ -664,6 +664,73 @@ int64_t orc_strand_run(const orc_strand_cfg *cfg, const uint8_t *ctype,
     return nrec;
 }
 
+/* OneD_VW.cc:199-349 (see lqt_oracle.h). */
+int64_t orc_vw_trial(const orc_strand_cfg *cfg, const uint8_t *ctype,
+                     const double *coeff, const lqt_model *m, double v0,
+                     double s2_time, double s2_dur, double s2_strength,
+                     int32_t s2_cell0, int32_t s2_ncells, double *max_endo,
+                     double *max_epi, double *rec, int64_t rec_cap)
+{
+    const int n = cfg->n;
+    const double dx = cfg->dx, dt = cfg->dt;
+    const double s2_base = (cfg->num_s1 - 1) * cfg->bcl;
+    double *s = (double *)malloc(sizeof(double) * LQT_NSTATE * n);
+    double *oldV = (double *)malloc(sizeof(double) * n);
+    double *dcoeff = (double *)malloc(sizeof(double) * n);
+    if (!s || !oldV || !dcoeff) {
+        free(s); free(oldV); free(dcoeff);
+        return -1;
+    }
+    for (int i = 0; i < n; ++i) orc_initial_state(v0, s + i * LQT_NSTATE);
+    for (int i = 0; i < n; ++i) {
+        if (n == 1) dcoeff[i] = 0.0;
+        else if (i == 0) dcoeff[i] = (coeff[i + 1] - coeff[i]) / dx;
+        else if (i == n - 1) dcoeff[i] = (coeff[i] - coeff[i - 1]) / dx;
+        else dcoeff[i] = (coeff[i + 1] - coeff[i - 1]) / (2.0 * dx);
+    }
+    double mendo = -100.0, mepi = -100.0;
+    int64_t nrec = 0;
+    double time;
+    int64_t step;
+    for (time = 0.0, step = 0; time <= cfg->stop_time; time += dt, step++) {
+        for (int i = 0; i < n; ++i) oldV[i] = s[i * LQT_NSTATE + LQT_S_V];
+        const int s1 = orc_in_window(time, cfg->bcl, cfg->stim_start, cfg->stim_dur);
+        const int s2 = !s1 && time - s2_base >= s2_time && time - s2_base < s2_time + s2_dur;
+#pragma omp parallel for schedule(static) if (n >= 64)
+        for (int i = 0; i < n; ++i) {
+            double ist = 0.0;
+            if (s1 && i < cfg->n_stim) ist = cfg->stim_strength;
+            else if (s2 && i >= s2_cell0 && i < s2_cell0 + s2_ncells) ist = s2_strength;
+            double fo, so;
+            if (n == 1) {
+                fo = so = 0.0;
+            } else if (i == 0) {
+                fo = (oldV[i + 1] - oldV[i]) / (1.0 * dx);
+                so = (oldV[i + 1] + oldV[i] - 2.0 * oldV[i]) / (dx * dx);
+            } else if (i < n - 1) {
+                fo = (oldV[i + 1] - oldV[i - 1]) / (2.0 * dx);
+                so = (oldV[i + 1] + oldV[i - 1] - 2.0 * oldV[i]) / (dx * dx);
+            } else {
+                fo = (oldV[i] - oldV[i - 1]) / (1.0 * dx);
+                so = (oldV[i] + oldV[i - 1] - 2.0 * oldV[i]) / (dx * dx);
+            }
+            orc_update(s + i * LQT_NSTATE, ctype[i], m, dt, ist, dcoeff[i] * fo + coeff[i] * so, NULL);
+        }
+        if (rec && floor(time / cfg->bcl) == cfg->num_s1 - 1 && step % 50 == 0 && nrec < rec_cap) {
+            for (int i = 0; i < n; ++i) rec[nrec * n + i] = s[i * LQT_NSTATE + LQT_S_V];
+            nrec++;
+        }
+        if (time - s2_base >= s2_time) {
+            if (s[(n - 1) * LQT_NSTATE + LQT_S_V] >= mepi) mepi = s[(n - 1) * LQT_NSTATE + LQT_S_V];
+            if (s[LQT_S_V] >= mendo) mendo = s[LQT_S_V];
+        }
+    }
+    if (max_endo) *max_endo = mendo;
+    if (max_epi) *max_epi = mepi;
+    free(s); free(oldV); free(dcoeff);
+    return nrec;
+}
+
 /* The device AP detector restated in FP64 (see lqt_oracle.h). */
 typedef struct {
     double vrest, vpeak, dvdt_max, t_act;

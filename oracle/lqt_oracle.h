@@ -79,6 +79,21 @@ int64_t orc_strand_run(const orc_strand_cfg *cfg, const uint8_t *ctype,
                        int64_t rec_cap, int32_t max_beats, double *act,
                        double *cv_out, double *final_state, int nthreads);
 
+/* One trial of the S1-S2 vulnerable-window search, OneD_VW.cc:199-349: a
+ * fresh strand; S1 on cells [0, n_stim) in the window of every cycle
+ * (stim_start, stim_dur, stim_strength); otherwise S2 on cells
+ * [s2_cell0, s2_cell0 + s2_ncells) while t - (num_s1 - 1) * bcl is in
+ * [s2_time, s2_time + s2_dur); steps while t <= stop_time.  Out: the
+ * maximum V of the first and the last cell over the steps with
+ * t - (num_s1 - 1) * bcl >= s2_time, starting at -100 (maxEndo, maxEpi), and
+ * optionally V of every cell every 50 steps of cycle num_s1 - 1 (the
+ * Transmural1D file rows).  Returns the rows written. */
+int64_t orc_vw_trial(const orc_strand_cfg *cfg, const uint8_t *ctype,
+                     const double *coeff, const lqt_model *m, double v0,
+                     double s2_time, double s2_dur, double s2_strength,
+                     int32_t s2_cell0, int32_t s2_ncells, double *max_endo,
+                     double *max_epi, double *rec, int64_t rec_cap);
+
 /* AP detector per cell and cycle, the definition the device kernels use:
  * on the step where a cycle's S1 window opens, rest = V before that step; an
  * upward crossing of act_thr marks activation; the upstroke ends at the first

@@ -103,6 +103,10 @@ def lib():
         L.orc_strand_detect.argtypes = [C.POINTER(StrandCfg), C.c_int32, P, P, C.POINTER(Model), C.c_double,
                                         C.c_int32, P, P, P, P, P]
         L.orc_strand_detect.restype = C.c_int64
+        L.orc_vw_trial.argtypes = [C.POINTER(StrandCfg), P, P, C.POINTER(Model), C.c_double, C.c_double, C.c_double,
+                                   C.c_double, C.c_int32, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double), P,
+                                   C.c_int64]
+        L.orc_vw_trial.restype = C.c_int64
         L.orc_ecg_1d.argtypes = [C.c_int32, P, C.c_double, C.c_double]
         L.orc_ecg_1d.restype = C.c_double
         L.orc_build_map.argtypes = [C.c_int32, C.c_int32, C.c_int32, P, P]
@@ -191,6 +195,24 @@ def strand_detect(types, coeff, m: Model, *, dx=0.15, dt=0.02, bcl=1000.0, stim_
     lib().orc_strand_detect(C.byref(cfg), s1_beats, _p(types), _p(coeff), C.byref(m), v0, max_beats, _p(t_act),
                             _p(apd), _p(ead), _p(nact), _p(fin))
     return dict(t_act=t_act, apd90=apd, ead=ead, nact=nact, final=fin)
+
+
+def vw_trial(types, coeff, m: Model, s2_time, *, dx=0.15, dt=0.02, bcl=1000.0, num_s1=5, stim_start=0.0,
+             stim_dur=3.0, stim_strength=-52.0, n_stim=3, s2_dur=3.0, s2_strength=-104.0, s2_cell0=10, s2_ncells=3,
+             v0=-87.5, record=False):
+    """One trial of OneD_VW.cc's S1-S2 search (FP64): (maxEndo, maxEpi[, final-cycle V rows])."""
+    types = np.ascontiguousarray(types, dtype=np.uint8)
+    coeff = np.ascontiguousarray(coeff, dtype=np.float64)
+    n = len(types)
+    cfg = StrandCfg(n, dx, dt, bcl, stim_start, stim_dur, stim_strength, n_stim, num_s1, num_s1 * bcl, -30.0)
+    me, mp = C.c_double(), C.c_double()
+    cap = int(bcl / (50 * dt)) + 2 if record else 0
+    rec = np.zeros((max(cap, 1), n))
+    nr = lib().orc_vw_trial(C.byref(cfg), _p(types), _p(coeff), C.byref(m), v0, s2_time, s2_dur, s2_strength,
+                            s2_cell0, s2_ncells, C.byref(me), C.byref(mp), _p(rec) if record else None, cap)
+    if record:
+        return me.value, mp.value, rec[:nr]
+    return me.value, mp.value
 
 
 def ecg_1d(v, dx=0.15, x0=35.0):
