@@ -202,3 +202,34 @@ def suprep_sweep(doses=tuple(range(0, 160, 10)), *, precision=N.MIXED, bcl=1000.
         out.append(dict(dose=float(d), t=rec["t"], ecg=rec["ecg"], qt=qt, t_peak=tpk, apd90=apd_last))
     b.close()
     return dict(results=out, device_ms=ms)
+
+
+def main():
+    """python -m lqt1_gb300.protocols vw|suprep [--fp64] [--out DIR]: one JSON line."""
+    import argparse
+    import json
+    ap = argparse.ArgumentParser()
+    ap.add_argument("what", choices=["vw", "suprep"])
+    ap.add_argument("--fp64", action="store_true")
+    ap.add_argument("--out", default=None, help="directory for the .dat files")
+    a = ap.parse_args()
+    prec = N.FP64 if a.fp64 else N.MIXED
+    if a.what == "vw":
+        t, r = vw_search(precision=prec)
+        out = {"protocol": "OneD_VW.cc MODE2 S1-S2 search", "first_vulnerable_s2_ms": t,
+               "timings_in_launch": int(len(r["s2"])), "device_ms": r["device_ms"],
+               "cell_steps_per_s": r["cell_steps"] / (r["device_ms"] / 1e3),
+               "window_ms": [float(r["s2"][r["vulnerable"]].min()), float(r["s2"][r["vulnerable"]].max())]
+               if r["vulnerable"].any() else None}
+        if t is not None and a.out:
+            write_vw_dat(os.path.join(a.out, "Transmural1D_s2@%.2f.dat" % t), vw_final_cycle(t, precision=prec))
+    else:
+        r = suprep_sweep(precision=prec, out_dir=a.out)
+        out = {"protocol": "SUPREP dose series, LQT1 + ISO1 strand", "device_ms": r["device_ms"],
+               "dose_fmol": [x["dose"] for x in r["results"]], "qt_ms": [x["qt"] for x in r["results"]],
+               "apd90_median_ms": [float(np.median(x["apd90"])) for x in r["results"]]}
+    print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()
