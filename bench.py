@@ -232,6 +232,7 @@ def main():
 
     import torch
     import lqt1_gb300 as lq
+    from lqt1_gb300 import replicas
     from lqt1_gb300 import surrogate as S
 
     if world > 1:
@@ -267,11 +268,7 @@ def main():
         e1.record(stream)
         torch.cuda.synchronize()
         barrier()
-        ms = e0.elapsed_time(e1)
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+        _, ms, _ = replicas.aggregate_throughput(float(sim.n) * steps, e0.elapsed_time(e1))
         return ms
 
     # ---- headline: FP32 + surrogate form -----------------------------------
@@ -372,12 +369,19 @@ def main():
     sweep = None
     if args.sweep_beats > 0:
         insts, models, _ = lq.batch.sweep(n=4096, seed=2024, beats=args.sweep_beats)
-        bt = lq.Batch(insts, models, precision=lq.MIXED, max_beats=args.sweep_beats + 1,
+        # ranks take contiguous shards of about equal work (no data collective)
+        wk = [len(x.types) * round(x.t_stop / 0.02) for x in insts]
+        lo, hi = replicas.shard_bounds(len(insts), rank, world, wk)
+        mine = insts[lo:hi]
+        for j, x in enumerate(mine):
+            x.model = j
+        bt = lq.Batch(mine, models[lo:hi], precision=lq.MIXED, max_beats=args.sweep_beats + 1,
                       stream=stream.cuda_stream)
-        work = sum(len(x.types) * round(x.t_stop / 0.02) for x in insts)
-        ms_sw = bt.run()
-        sweep = {"value": world * work / (ms_sw / 1e3), "unit": UNIT, "instances": len(insts), "cells": bt.ncells,
-                 "beats": args.sweep_beats, "device_ms": ms_sw, "launch": bt.config(),
+        barrier()
+        ms_local = bt.run()
+        v_sw, ms_sw, work = replicas.aggregate_throughput(float(sum(wk[lo:hi])), ms_local)
+        sweep = {"value": v_sw, "unit": UNIT, "instances": len(insts), "cells": int(sum(len(x.types) for x in insts)),
+                 "beats": args.sweep_beats, "device_ms": ms_sw, "launch": bt.config(), "scaling": "strong",
                  "blowup_cell_steps": bt.num_bad(), "form": "mixed"}
         bt.close()
 
