@@ -49,7 +49,7 @@ struct lqt_mlp {
     DevMem ws;
     MlpDev dev() const
     {
-        return MlpDev{Pb + kOW1, Pb + kOW2, Pb + kOW3, P + kOB1, P + kOB2, P + kOB3};
+        return MlpDev{Pb + kOW1, Pb + kOW2, Pb + kOW3, P + kOB1, P + kOB2, P + kOB3, P + kOW2, P + kOW3};
     }
 };
 

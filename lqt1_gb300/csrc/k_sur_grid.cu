@@ -12,7 +12,7 @@
 //   2. one elected thread runs the 48 -> 128 -> 128 -> 48 network with
 //      tcgen05.mma into TMEM (three layers, each bias added by one more MMA
 //      k-step against a constant ones tile; the threads read the hidden
-//      accumulators back with tcgen05.ld, apply SiLU and write the next BF16
+//      accumulators back with tcgen05.ld, apply SiLU and write the next FP16
 //      operand into shared memory);
 //   3. each thread reloads its state, advances it by one coarse TPORd step of
 //      the macro length (dt = kSurSteps * dt, no diffusion) and adds the
@@ -36,6 +36,7 @@
 // warpgroups work on four tiles independently, synchronised by named
 // barriers.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -55,18 +56,22 @@ constexpr uint32_t kTmemCols = kColsPerGroup * kGroups;   // the SM's 512 column
 constexpr uint32_t kWaitLimit = 1u << 24;  // bounded mbarrier polls
 constexpr float kDetMargin = 2.f;          // mV a surrogate voxel cannot cover in one macro step
 
-constexpr uint32_t kOffW1 = 0;                                      // 128 x 48
-constexpr uint32_t kOffW2 = kOffW1 + kMlpHid * kMlpIn * 2;          // 128 x 128
-constexpr uint32_t kOffW3 = kOffW2 + kMlpHid * kMlpHid * 2;         // 48 x 128
-constexpr uint32_t kOffXH = kOffW3 + kMlpOut * kMlpHid * 2;         // per group: 128 x 128 BF16
+// Operand types: the first layer's inputs and weights are BF16; the hidden
+// layers' activations and weights are FP16 (finer rounding for the packed SiLU
+// below); accumulation is FP32 throughout.  No MMA mixes the two types.
+constexpr uint32_t kOffW1 = 0;                                      // 128 x 48 BF16
+constexpr uint32_t kOffW2 = kOffW1 + kMlpHid * kMlpIn * 2;          // 128 x 128 FP16
+constexpr uint32_t kOffW3 = kOffW2 + kMlpHid * kMlpHid * 2;         // 48 x 128 FP16
+constexpr uint32_t kOffXH = kOffW3 + kMlpOut * kMlpHid * 2;         // per group: BF16 features, then FP16 hidden
 constexpr uint32_t kXHBytes = kTile * kMlpHid * 2;
 // bias k-step operands (K = 16 core-matrix tiles): A = ones in columns 0, 1;
-// B = the bias split into BF16 hi + lo parts in columns 0, 1
+// B = the bias split into hi + lo parts in columns 0, 1
 constexpr uint32_t kBiasK = 16;
-constexpr uint32_t kOffOnes = kOffXH + kGroups * kXHBytes;          // 128 x 16
-constexpr uint32_t kOffB1 = kOffOnes + kTile * kBiasK * 2;          // 128 x 16 (b1 / 2)
-constexpr uint32_t kOffB2 = kOffB1 + kMlpHid * kBiasK * 2;          // 128 x 16 (b2 / 2)
-constexpr uint32_t kOffB3 = kOffB2 + kMlpHid * kBiasK * 2;          // 48 x 16 (b3)
+constexpr uint32_t kOffOnes = kOffXH + kGroups * kXHBytes;          // 128 x 16 BF16
+constexpr uint32_t kOffOnesH = kOffOnes + kTile * kBiasK * 2;       // 128 x 16 FP16
+constexpr uint32_t kOffB1 = kOffOnesH + kTile * kBiasK * 2;         // 128 x 16 (b1 / 2, BF16)
+constexpr uint32_t kOffB2 = kOffB1 + kMlpHid * kBiasK * 2;          // 128 x 16 (b2 / 2, FP16)
+constexpr uint32_t kOffB3 = kOffB2 + kMlpHid * kBiasK * 2;          // 48 x 16 (b3, FP16)
 constexpr uint32_t kOffNorm = kOffB3 + kMlpOut * kBiasK * 2;        // 4 x 48 floats
 constexpr uint32_t kOffBar = kOffNorm + 4 * kMlpIn * 4;             // per group mbarrier; tmem slot
 constexpr uint32_t kSmemBytes = kOffBar + 8 * kGroups + 16;
@@ -89,47 +94,69 @@ __device__ void stage_kmajor(uint8_t *dst, const __nv_bfloat16 *src, int R, int 
     }
 }
 
+// A row-major [R][K] FP32 matrix into the K-major core layout as FP16, times `scale`.
+__device__ void stage_kmajor_f16(uint8_t *dst, const float *src, int R, int K, float scale)
+{
+    const int chunks = R * (K / 8);
+    for (int c = threadIdx.x; c < chunks; c += blockDim.x) {
+        const int r = c / (K / 8), kg = c % (K / 8);
+        const float *s = src + (int64_t)r * K + kg * 8;
+        uint32_t p[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const __half2 h = __floats2half2_rn(scale * s[2 * i], scale * s[2 * i + 1]);
+            p[i] = *reinterpret_cast<const uint32_t *>(&h);
+        }
+        *reinterpret_cast<uint4 *>(dst + tc::kmaj_off(r, kg * 8, K)) = make_uint4(p[0], p[1], p[2], p[3]);
+    }
+}
+
 // Bias operand of the extra k-step: row n = (hi, lo, 0, ...) with
-// hi + lo = scale * b[n] to about 16 bits.
-__device__ void stage_bias(uint8_t *dst, const float *b, int N, float scale)
+// hi + lo = scale * b[n] to about twice the type's precision.
+template <bool F16> __device__ void stage_bias(uint8_t *dst, const float *b, int N, float scale)
 {
     for (int c = threadIdx.x; c < N * 2; c += blockDim.x) {
         const int n = c >> 1, kg = c & 1;
         uint4 v = make_uint4(0, 0, 0, 0);
         if (kg == 0) {
             const float x = scale * b[n];
-            const __nv_bfloat16 hi = __float2bfloat16_rn(x);
-            const __nv_bfloat16 lo = __float2bfloat16_rn(x - __bfloat162float(hi));
-            v.x = (uint32_t)__bfloat16_as_ushort(hi) | ((uint32_t)__bfloat16_as_ushort(lo) << 16);
+            if (F16) {
+                const __half hi = __float2half_rn(x);
+                const __half lo = __float2half_rn(x - __half2float(hi));
+                v.x = (uint32_t)__half_as_ushort(hi) | ((uint32_t)__half_as_ushort(lo) << 16);
+            } else {
+                const __nv_bfloat16 hi = __float2bfloat16_rn(x);
+                const __nv_bfloat16 lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+                v.x = (uint32_t)__bfloat16_as_ushort(hi) | ((uint32_t)__bfloat16_as_ushort(lo) << 16);
+            }
         }
         *reinterpret_cast<uint4 *>(dst + tc::kmaj_off(n, kg * 8, kBiasK)) = v;
     }
 }
 
-// SiLU of two hidden pre-activations, packed to the BF16 operand of the next
+// SiLU of two hidden pre-activations, packed to the FP16 operand of the next
 // layer: the hidden layers run with halved weights and biases, so the
-// accumulator is h = x / 2 and SiLU(x) = x * sigmoid(x) = h + h * tanh(h); one
-// MUFU tanh.approx.f32 per value (relative error about 2^-11, below the BF16
-// rounding that follows).
-__device__ __forceinline__ float tanh_fast(float x)
+// accumulator is h = x / 2 and SiLU(x) = x * sigmoid(x) = h + h * tanh(h).  h
+// is rounded once to FP16, then one MUFU tanh.approx.f16x2 and one
+// fma.rn.f16x2 produce the pair (three instructions for two values).
+__device__ __forceinline__ uint32_t silu2_f16(float h0, float h1)
 {
-    float t;
-    asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(x));
-    return t;
-}
-__device__ __forceinline__ uint32_t silu2_bf16(float h0, float h1)
-{
-    const __nv_bfloat162 r = __floats2bfloat162_rn(fmaf(h0, tanh_fast(h0), h0), fmaf(h1, tanh_fast(h1), h1));
+    const __half2 h = __floats2half2_rn(h0, h1);
+    const uint32_t hu = *reinterpret_cast<const uint32_t *>(&h);
+    uint32_t tu;
+    asm("tanh.approx.f16x2 %0, %1;" : "=r"(tu) : "r"(hu));
+    const __half2 r = __hfma2(h, *reinterpret_cast<const __half2 *>(&tu), h);
     return *reinterpret_cast<const uint32_t *>(&r);
 }
 
 // D[128 x N] = A[128 x K] * B[N x K]^T + ones * bias^T: K / 16 MMAs over the
-// operands, then one k-step of the constant ones tile against the bias tile.
+// operands, then one k-step of the constant ones tile against the bias tile;
+// every operand of the call is BF16 (f16 = false) or every one FP16.
 __device__ __forceinline__ void gemm(uint32_t tmem_d, const uint8_t *A, const uint8_t *B, int K, int N,
-                                     const uint8_t *ones, const uint8_t *bias)
+                                     const uint8_t *ones, const uint8_t *bias, bool f16)
 {
     const uint32_t lbo = 128, sbo = (uint32_t)(K / 8) * 128;
-    const uint32_t id = tc::idesc_bf16_f32(128, N);
+    const uint32_t id = f16 ? tc::idesc_f16_f32(128, N) : tc::idesc_bf16_f32(128, N);
     const uint32_t a0 = tc::smem_u32(A), b0 = tc::smem_u32(B);
     for (int kk = 0; kk < K / 16; ++kk) {
         const uint32_t step = (uint32_t)kk * 256;     // two core matrices along K
@@ -218,16 +245,18 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
     if (use_net) {
         // hidden layers halved (see silu2_bf16); biases as an extra k-step
         stage_kmajor(smem + kOffW1, sg.w.w1t, kMlpHid, kMlpIn, 0.5f);
-        stage_kmajor(smem + kOffW2, sg.w.w2t, kMlpHid, kMlpHid, 0.5f);
-        stage_kmajor(smem + kOffW3, sg.w.w3t, kMlpOut, kMlpHid, 1.0f);
-        stage_bias(smem + kOffB1, sg.w.b1, kMlpHid, 0.5f);
-        stage_bias(smem + kOffB2, sg.w.b2, kMlpHid, 0.5f);
-        stage_bias(smem + kOffB3, sg.w.b3, kMlpOut, 1.0f);
+        stage_kmajor_f16(smem + kOffW2, sg.w.w2f, kMlpHid, kMlpHid, 0.5f);
+        stage_kmajor_f16(smem + kOffW3, sg.w.w3f, kMlpOut, kMlpHid, 1.0f);
+        stage_bias<false>(smem + kOffB1, sg.w.b1, kMlpHid, 0.5f);
+        stage_bias<true>(smem + kOffB2, sg.w.b2, kMlpHid, 0.5f);
+        stage_bias<true>(smem + kOffB3, sg.w.b3, kMlpOut, 1.0f);
         for (int c = tid; c < kTile * 2; c += blockDim.x) {
             const int r = c >> 1, kg = c & 1;
-            const uint32_t one = 0x3F80u;                // BF16 1.0
-            const uint4 v = kg == 0 ? make_uint4(one | (one << 16), 0, 0, 0) : make_uint4(0, 0, 0, 0);
-            *reinterpret_cast<uint4 *>(smem + kOffOnes + tc::kmaj_off(r, kg * 8, kBiasK)) = v;
+            const uint32_t one_b = 0x3F80u, one_h = 0x3C00u;     // 1.0 in BF16, FP16
+            const uint4 vb = kg == 0 ? make_uint4(one_b | (one_b << 16), 0, 0, 0) : make_uint4(0, 0, 0, 0);
+            const uint4 vh = kg == 0 ? make_uint4(one_h | (one_h << 16), 0, 0, 0) : make_uint4(0, 0, 0, 0);
+            *reinterpret_cast<uint4 *>(smem + kOffOnes + tc::kmaj_off(r, kg * 8, kBiasK)) = vb;
+            *reinterpret_cast<uint4 *>(smem + kOffOnesH + tc::kmaj_off(r, kg * 8, kBiasK)) = vh;
         }
         if (t == 0) {
             tc::mbar_init(bar, 1);
@@ -267,20 +296,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
     // operand buffer); the loop is uniform within a warpgroup
     for (int64_t tile = (int64_t)blockIdx.x * kGroups + grp; tile < ntiles; tile += tstride) {
         const int64_t k = tile * kTile + t;
-        // the next tile's state lines into L2 (one 128-byte line per array
-        // and warp: lane L takes state arrays L and 32 + L)
-        {
-            const int64_t kn = (tile + tstride) * kTile + (warp & 3) * 32;
-            if (kn < nt) {
-                const int64_t ld = gd.s.ld;
-                const float *cf = reinterpret_cast<const float *>(gd.s.conc);
-#pragma unroll
-                for (int a = lane; a < 16 + 29; a += 32) {
-                    const float *p = a < 16 ? cf + a * ld + kn : gd.s.gate + ((a - 16) < 3 ? a - 16 : a - 14) * ld + kn;
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-                }
-            }
-        }
         bool elig = false, need_det = false;
         float vc = 0.f;
         int ct = 0;
@@ -354,10 +369,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
             for (int layer = 0; layer < 3; ++layer) {
                 if (t == 0) {
                     tc::fence_after();
-                    if (layer == 0) gemm(t_acc_mma, xh, smem + kOffW1, kMlpIn, kMlpHid, smem + kOffOnes, smem + kOffB1);
+                    if (layer == 0)
+                        gemm(t_acc_mma, xh, smem + kOffW1, kMlpIn, kMlpHid, smem + kOffOnes, smem + kOffB1, false);
                     else if (layer == 1)
-                        gemm(t_acc_mma, xh, smem + kOffW2, kMlpHid, kMlpHid, smem + kOffOnes, smem + kOffB2);
-                    else gemm(t_acc_mma, xh, smem + kOffW3, kMlpHid, kMlpOut, smem + kOffOnes, smem + kOffB3);
+                        gemm(t_acc_mma, xh, smem + kOffW2, kMlpHid, kMlpHid, smem + kOffOnesH, smem + kOffB2, true);
+                    else gemm(t_acc_mma, xh, smem + kOffW3, kMlpHid, kMlpOut, smem + kOffOnesH, smem + kOffB3, true);
                     tc::mma_commit(bar);
                 }
                 // every thread of the group takes the same branch: a wait that
@@ -372,7 +388,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
                 phase ^= 1;
                 tc::fence_after();
                 if (layer == 2) break;
-                // hidden layer: TMEM -> SiLU -> BF16 operand (over the feature
+                // hidden layer: TMEM -> SiLU -> FP16 operand (over the feature
                 // tile, which the finished MMA no longer needs)
 #pragma unroll 1
                 for (int cc = 0; cc < kMlpHid; cc += 32) {
@@ -382,7 +398,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
                     for (int q = 0; q < 4; ++q) {
                         uint32_t packed[4];
 #pragma unroll
-                        for (int i = 0; i < 4; ++i) packed[i] = silu2_bf16(v[q * 8 + 2 * i], v[q * 8 + 2 * i + 1]);
+                        for (int i = 0; i < 4; ++i) packed[i] = silu2_f16(v[q * 8 + 2 * i], v[q * 8 + 2 * i + 1]);
                         *reinterpret_cast<uint4 *>(xh + tc::kmaj_off(t, cc + q * 8, kMlpHid)) =
                             make_uint4(packed[0], packed[1], packed[2], packed[3]);
                     }

@@ -19,6 +19,7 @@ constexpr int kMlpNState = 38, kMlpNParam = 6;
 struct MlpDev {
     const __nv_bfloat16 *w1t, *w2t, *w3t;   // [128][48], [128][128], [48][128]
     const float *b1, *b2, *b3;              // [128], [128], [48]
+    const float *w2f, *w3f;                 // FP32 master copies of W2, W3
 };
 
 }  // namespace lqt

@@ -39,6 +39,11 @@ __host__ __device__ __forceinline__ uint32_t idesc_bf16_f32(int M, int N)
 {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
+// The same with A = B = F16 (type fields 0).  One MMA never mixes the two types.
+__host__ __device__ __forceinline__ uint32_t idesc_f16_f32(int M, int N)
+{
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
 
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
 {
