@@ -312,10 +312,12 @@ int lqt_sim_get_detect(lqt_sim *s, float *t_act_host, float *apd90_host,
 
 /* Occupancy variant of the fused step kernel: the minimum resident CTAs/SM its
  * register allocation allows (mixed form 2, 3, 4; FP64 1, 2).  variant >= 0
- * forces one; variant < 0 runs the autotuner now (15 real steps, each variant
- * timed with CUDA events, the fastest kept).  The first lqt_sim_step call with
- * nsteps >= 64 autotunes by itself unless a variant was forced.  All variants
- * give bit-identical results.  ms_per_variant: up to 4 timings (or NULL). */
+ * forces one; variant < 0 runs the autotuner now (15 real steps, the variants
+ * in turn, each timed with CUDA events, the fastest kept; with a surrogate
+ * attached, 15 more steps pick the variant of the V-only substep kernel).  The
+ * first lqt_sim_step call with nsteps >= 64 autotunes by itself unless a
+ * variant was forced.  All variants give bit-identical results.
+ * ms_per_variant: up to 4 timings (or NULL). */
 int lqt_sim_tune(lqt_sim *s, int32_t variant, int32_t *chosen, float *ms_per_variant);
 
 /* Instrumentation (no counterpart in the reference, which has no timing):

@@ -76,6 +76,7 @@ struct lqt_sim {
     int64_t *ecg_count = nullptr, ecg_cap = 0;
     // occupancy variant of k_grid_step (minimum CTAs/SM) and the autotuner
     int minb = 2;
+    int sub_minb = 5;               // k_sur_substep occupancy variant
     bool tuned = false;
     float tune_ms[4] = {0, 0, 0, 0};
     // learned surrogate (mixed form): network, per-voxel rate, counters
@@ -263,7 +264,7 @@ cudaError_t launch_substep(lqt_sim *s)
     if (s->fp64()) return launch_grid_step<double>(devf<double>(s), k, s->cur, s->dim, s->minb, s->stream);
     const GridDev<float> g = devf<float>(s);
     if (g.srate) {
-        cudaError_t e = launch_sur_substep(g, s->p.dt, s->cur, s->dim, s->stream);
+        cudaError_t e = launch_sur_substep(g, s->p.dt, s->cur, s->dim, s->sub_minb, s->stream);
         if (e != cudaSuccess) return e;
     }
     return launch_grid_step<float>(g, k, s->cur, s->dim, s->minb, s->stream);
@@ -358,9 +359,44 @@ int autotune(lqt_sim *s, int per, int64_t *consumed)
             best_m = cand[c];
         }
     }
+    s->minb = best_m;
+    // with a surrogate attached: the V-only substep's variant, timed the same
+    // way (variants in turn, whole steps, the first round discarded)
+    if (rc == LQT_OK && s->sur && !s->fp64()) {
+        float ts[3] = {0, 0, 0};
+        for (int i = 0; i < per && rc == LQT_OK; ++i) {
+            for (int c = 0; c < 3 && rc == LQT_OK; ++c) {
+                s->sub_minb = kSubVariants[c];
+                rc = launch_sur_if_due(s);
+                if (rc) break;
+                const GridDev<float> g = devf<float>(s);
+                cudaError_t e = cudaEventRecord(a, s->stream);
+                if (e == cudaSuccess && g.srate) e = launch_sur_substep(g, s->p.dt, s->cur, s->dim, s->sub_minb, s->stream);
+                if (e == cudaSuccess) e = cudaEventRecord(b, s->stream);
+                if (e == cudaSuccess) e = launch_grid_step<float>(g, make_stepk(s->p.dt), s->cur, s->dim, s->minb, s->stream);
+                if (e == cudaSuccess) e = launch_ghost_now(s);
+                if (e == cudaSuccess) e = cudaEventSynchronize(b);
+                float ms = 0.f;
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+                if (e != cudaSuccess) {
+                    rc = fail(LQT_ERR_CUDA, std::string("autotune: ") + cudaGetErrorString(e));
+                    break;
+                }
+                s->cur ^= 1;
+                s->step += 1;
+                s->time += s->p.dt;
+                ++*consumed;
+                if (s->nel > 0 && s->ecg_every > 0 && s->step % s->ecg_every == 0) rc = launch_ecg_now(s);
+                if (i > 0) ts[c] += ms;
+            }
+        }
+        int bs = 0;
+        for (int c = 1; c < 3; ++c)
+            if (ts[c] < ts[bs]) bs = c;
+        s->sub_minb = kSubVariants[bs];
+    }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    s->minb = best_m;
     s->tuned = true;
     s->graph_valid = false;
     return rc;

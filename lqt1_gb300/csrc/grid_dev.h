@@ -70,7 +70,9 @@ cudaError_t launch_grid_step(const GridDev<R> &gd, const StepK &k, int cur, int 
 template <typename R>
 cudaError_t launch_grid_step_minb(const GridDev<R> &gd, const StepT<R> &k, int cur, int dim, int minb, cudaStream_t st);
 template <typename R> cudaError_t launch_ghost(const GridDev<R> &gd, int nxt, cudaStream_t st);
-cudaError_t launch_sur_substep(const GridDev<float> &gd, double dt, int cur, int dim, cudaStream_t st);
+// Occupancy variants of k_sur_substep: minimum CTAs/SM of 256 threads.
+constexpr int kSubVariants[3] = {5, 6, 8};
+cudaError_t launch_sur_substep(const GridDev<float> &gd, double dt, int cur, int dim, int minb, cudaStream_t st);
 template <typename R>
 cudaError_t launch_ecg(const GridDev<R> &gd, int cur, const float4 *el, int nel, double *partial, double *out,
                        double *t_out, int64_t *counter, int64_t cap, int dim, cudaStream_t st);

@@ -203,7 +203,10 @@ __device__ __forceinline__ float sub_du(const GridDev<float> &gd, const float *_
     return du;
 }
 
-template <int DIM> __global__ void __launch_bounds__(256) k_sur_substep(GridDev<float> gd, float dt, int cur)
+// MINB: minimum resident CTAs per SM (occupancy variants, picked at run time
+// by the autotuner; 5 / 6 / 8 CTAs of 256 threads = 48 / 40 / 32 registers).
+template <int DIM, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_sur_substep(GridDev<float> gd, float dt, int cur)
 {
     const int64_t k0 = blockIdx.x * (int64_t)(blockDim.x * kSubU) + threadIdx.x;
     const bool aniso = DIM > 1 && gd.d6;
@@ -224,10 +227,16 @@ template <int DIM> __global__ void __launch_bounds__(256) k_sur_substep(GridDev<
 #pragma unroll
         for (int i = 0; i < 3; ++i) Bt[u][i] = 0.f;
         if (aniso && on[u]) {
+            // streamed once per step: evict-first, the L2 is for the V rows
+            const float2 *d2 = reinterpret_cast<const float2 *>(gd.d6 + 6 * k);   // 24-byte rows: 8-byte aligned
 #pragma unroll
-            for (int i = 0; i < (DIM == 3 ? 6 : 4); ++i) Dt[u][i] = __ldg(gd.d6 + 6 * k + i);
+            for (int i = 0; i < (DIM == 3 ? 3 : 2); ++i) {
+                const float2 q = __ldcs(d2 + i);
+                Dt[u][2 * i] = q.x;
+                Dt[u][2 * i + 1] = q.y;
+            }
 #pragma unroll
-            for (int i = 0; i < (DIM == 3 ? 3 : 2); ++i) Bt[u][i] = __ldg(gd.b3 + 3 * k + i);
+            for (int i = 0; i < (DIM == 3 ? 3 : 2); ++i) Bt[u][i] = __ldcs(gd.b3 + 3 * k + i);
         }
     }
     bool any = false;
