@@ -12,7 +12,16 @@ from .cell import STATE_NAMES, TPORdCells, initial_state  # noqa: F401
 
 __all__ = ["TPORdCells", "Batch", "InstanceSpec", "OneDStrand", "oned_types", "initial_state", "model", "lib",
            "Model", "LqtError", "FP64", "MIXED", "LVEPI", "LVENDO", "EPI", "ENDO", "MCELL", "EMPTY", "STATE_NAMES"]
-from . import batch, geometry, protocols  # noqa: E402,F401
+from . import batch, geometry  # noqa: E402,F401
 from .sim import Sim  # noqa: E402,F401
 
 __all__ += ["Sim", "geometry"]
+
+
+def __getattr__(name):
+    # protocols, surrogate, replicas load on first use (and run as
+    # `python -m lqt1_gb300.<module>` without a second import)
+    if name in ("protocols", "surrogate", "replicas"):
+        import importlib
+        return importlib.import_module("." + name, __name__)
+    raise AttributeError(name)

@@ -35,23 +35,27 @@ def test_vw_trials_match_oracle(lq, orc):
 
 
 def test_vw_search_finds_the_oracles_window(lq, orc):
-    """MODE2 search (S2 from 260 ms upward in 0.1 ms steps) as batched
-    launches.  The mixed form locates the window over 1000 timings in one
-    launch; the FP64 batch and the oracle agree on the first vulnerable
-    timing: vulnerable there, not 0.1 ms earlier."""
-    t_mx, _ = lq.protocols.vw_search(start=260.0, step=0.1, batch=1000, max_batches=2, precision=lq.MIXED)
-    assert t_mx is not None
-    lo = max(260.0, round(t_mx - 2.0, 1))
-    t64, r64 = lq.protocols.vw_search(start=lo, step=0.1, batch=41, max_batches=1, precision=lq.FP64)
-    assert t64 is not None and abs(t64 - t_mx) <= 1.0
+    """MODE2 search (S2 timings upward in 0.1 ms steps) as batched launches,
+    from 200 ms so that the window's opening lies inside the scan.  The mixed
+    form scans 1000 timings in one launch; the FP64 batch and the oracle agree
+    on the edges: vulnerable at the first and the last timing of the window,
+    not 0.1 ms outside either."""
+    t_mx, r_mx = lq.protocols.vw_search(start=200.0, step=0.1, batch=1000, max_batches=1, precision=lq.MIXED)
+    assert t_mx is not None and t_mx > 200.0
+    vul = r_mx["s2"][r_mx["vulnerable"]]
+    lo = round(t_mx - 1.0, 1)
+    t64, r64 = lq.protocols.vw_search(start=lo, step=0.1, batch=21, max_batches=1, precision=lq.FP64)
+    assert t64 is not None and abs(t64 - t_mx) <= 0.5
+    hi_mx = float(vul.max())
+    r64b = lq.protocols.vulnerable_window(np.round(hi_mx + 0.1 * np.arange(-10, 11), 1), precision=lq.FP64)
+    hi64 = float(r64b["s2"][r64b["vulnerable"]].max())
+    assert abs(hi64 - hi_mx) <= 0.5
     types = lq.protocols.vw_types()
     coeff = lq.protocols.vw_coeff()
     m = orc.model("default")
-    me, mp = orc.vw_trial(types, coeff, m, t64)
-    assert (me + 10) * (mp + 10) <= 0
-    if t64 - 0.1 >= 260.0 - 1e-9:
-        me0, mp0 = orc.vw_trial(types, coeff, m, round(t64 - 0.1, 1))
-        assert (me0 + 10) * (mp0 + 10) > 0
+    for t, inside in ((t64, True), (round(t64 - 0.1, 1), False), (hi64, True), (round(hi64 + 0.1, 1), False)):
+        me, mp = orc.vw_trial(types, coeff, m, t)
+        assert ((me + 10) * (mp + 10) <= 0) == inside, (t, me, mp)
 
 
 def test_vw_final_cycle_file(lq, orc, tmp_path):
