@@ -137,6 +137,80 @@ def generate(ncells=65536, seed=1, cap=20_000_000, *, gks=(0.05, 1.0), pca=(1.0,
     return X[:n.value], D[:n.value]
 
 
+# network order of the 38 evolving states -> index in the 40-state vector
+REF_INDEX = [0] + list(range(1, 9)) + [9 + (j if j < 3 else j + 2) for j in range(29)]
+
+
+def tissue_pairs(n_target=6_000_000, *, sheets=4, n=160, t_end=900.0, grab_every=2.0, dvdt_max=2.0, seed=7,
+                 gks=(0.05, 1.0), pca=(1.0, 2.2), iso=(1.0, 2.0), log=print):
+    """Training pairs from tissue: 2D sheets in the layout of the 600 x 600
+    S1-S2 workload (n x n at 0.15 mm, endo/M/epi bands, S1 line, S2 quadrant at
+    a seeded coupling interval U[300, 360] ms), each with a seeded model, run
+    with the plain mixed-form integrator.  Every `grab_every` ms the voxels
+    with |dV/dt| <= dvdt_max over the last step are sampled; the targets are
+    computed on the GPU from those states exactly as k_sur_datagen computes
+    them (5 plain steps of 0.02 ms minus one coarse step of 0.1 ms, no
+    diffusion, no stimulus).  Returns torch tensors X [m, 44], D [m, 38]."""
+    import torch
+
+    from . import geometry
+    from .cell import TPORdCells
+    from .sim import Sim
+    rng = np.random.default_rng(seed)
+    X, D = [], []
+    per_sheet = n_target // sheets
+    for k in range(sheets):
+        g_ = float(rng.uniform(*gks))
+        p_ = float(rng.uniform(*pca))
+        i_ = float(rng.uniform(*iso))
+        m = N.model("baseline", gks_scale=g_, pca_scale=p_, gks_iso_scale=i_)
+        sh = geometry.sheet(n, n, s1_cols=3)
+        ci = float(rng.uniform(300.0, 360.0))
+        sim = Sim(sh.types, 0.15, precision=N.MIXED, model=m)
+        sim.set_protocol(bcl=1000.0, s1_mask=sh.s1_mask, s1_start=0.0, s1_duration=2.0, s1_strength=-52.0,
+                         s1_beats=1, s2_time=ci, s2_duration=3.0, s2_strength=-104.0, s2_mask=sh.s2_mask)
+        types = sh.types.reshape(-1)[sim.tissue_index()]
+        cls = np.where(types == N.EPI, 1, np.where(types == N.MCELL, 2, 0))
+        every = int(round(grab_every / 0.02))
+        ngrab = int(t_end / grab_every)
+        take = min(1.0, per_sheet / (ngrab * sim.n * 0.85))
+        sel_states, sel_types, sel_cls = [], [], []
+        for _ in range(ngrab):
+            sim.step(every - 1)
+            v_prev = sim.get_v(as_double=True)
+            sim.step(1)
+            st = sim.get_state()
+            keep = (np.abs((st[:, 0] - v_prev) / 0.02) <= dvdt_max) & (rng.random(sim.n) < take)
+            sel_states.append(st[keep])
+            sel_types.append(types[keep])
+            sel_cls.append(cls[keep])
+        sim.close()
+        st = np.concatenate(sel_states)
+        ty = np.concatenate(sel_types)
+        cl = np.concatenate(sel_cls)
+        fine = TPORdCells(ty, precision=N.MIXED, model=m, dt=0.02)
+        fine.set_state(st)
+        fine.update(kSurStepsPy)
+        xf = fine.get_state()
+        fine.close()
+        coarse = TPORdCells(ty, precision=N.MIXED, model=m, dt=0.02 * kSurStepsPy)
+        coarse.set_state(st)
+        coarse.update(1)
+        xc = coarse.get_state()
+        coarse.close()
+        x = np.zeros((len(st), 44), np.float32)
+        x[:, :38] = st[:, REF_INDEX]
+        x[:, 38:41] = (g_, p_, i_)
+        x[np.arange(len(st)), 41 + cl] = 1.0
+        X.append(torch.from_numpy(x))
+        D.append(torch.from_numpy((xf - xc)[:, REF_INDEX].astype(np.float32)))
+        log(f"tissue sheet {k}: model gks {g_:.2f} pca {p_:.2f} iso {i_:.2f}, S2 at {ci:.1f} ms, {len(st)} pairs")
+    return torch.cat(X).cuda(), torch.cat(D).cuda()
+
+
+kSurStepsPy = 5
+
+
 def fit_bounds(D, out_scale):
     """Largest |normalised target| of each output over the whole set (the
     residual bounds); outputs without a target get 1."""
@@ -245,16 +319,27 @@ def load(path: str | None = None, stream: int | None = None) -> Mlp:
 
 
 def train_default(out=DEFAULT_WEIGHTS, *, ncells=65536, cap=20_000_000, prob=0.005, epochs=12, batch=8192,
-                  lr=2e-3, seed=1, log=print):
-    """Generate the pairs, fit the normalisation, train, validate, save."""
+                  lr=2e-3, seed=1, tissue=0, log=print):
+    """Generate the pairs (paced single cells with the sweep's parameter
+    ranges, plus `tissue` pairs from 2D S1-S2 sheets), fit the normalisation,
+    train, validate, save."""
     import time
 
     import torch
     t0 = time.perf_counter()
-    X, D = generate(ncells=ncells, cap=cap, prob=prob, seed=seed)
+    X, D = generate(ncells=ncells, cap=cap - tissue, prob=prob * (cap - tissue) / cap, seed=seed)
+    if tissue > 0:
+        Xt, Dt = tissue_pairs(tissue, seed=seed + 6, log=log)
+        X, D = torch.cat([X, Xt]), torch.cat([D, Dt])
+        del Xt, Dt
+        # one shuffle, so that the held-out tail mixes both sources
+        g = torch.Generator(device="cuda").manual_seed(seed)
+        perm = torch.randperm(X.shape[0], device="cuda", generator=g)
+        X, D = X[perm], D[perm]
+        del perm
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    log(f"pairs {X.shape[0]} in {t1 - t0:.1f} s")
+    log(f"pairs {X.shape[0]} ({X.shape[0] - tissue if tissue else X.shape[0]} single-cell) in {t1 - t0:.1f} s")
     m = Mlp(seed=seed)
     im, isc, osc = fit_norm(X, D)
     m.set_norm(im, isc, osc)
@@ -263,7 +348,8 @@ def train_default(out=DEFAULT_WEIGHTS, *, ncells=65536, cap=20_000_000, prob=0.0
     torch.cuda.synchronize()
     t2 = time.perf_counter()
     rel = val["rmse"] / np.maximum(val["zero_rmse"], 1e-30)
-    meta = dict(pairs=int(X.shape[0]), ncells=ncells, epochs=epochs, batch=batch, lr=lr, seed=seed, dt=0.02,
+    meta = dict(pairs=int(X.shape[0]), tissue_pairs=int(tissue), ncells=ncells, epochs=epochs, batch=batch, lr=lr,
+                seed=seed, dt=0.02,
                 macro_steps=5, gen_s=t1 - t0, train_s=t2 - t1, loss_history=[(int(k), float(l)) for k, l in hist],
                 val_rmse=val["rmse"].tolist(), val_zero_rmse=val["zero_rmse"].tolist(), val_n=int(val["n"]),
                 state_names=STATE_NAMES)
@@ -292,9 +378,10 @@ def main():
     ap.add_argument("--batch", type=int, default=8192)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--tissue", type=int, default=0, help="pairs from 2D S1-S2 sheets mixed in (0 = none)")
     a = ap.parse_args()
     train_default(a.out, ncells=a.cells, cap=a.pairs, prob=a.prob, epochs=a.epochs, batch=a.batch, lr=a.lr,
-                  seed=a.seed, log=lambda m: print(m, flush=True))
+                  seed=a.seed, tissue=a.tissue, log=lambda m: print(m, flush=True))
 
 
 if __name__ == "__main__":
