@@ -294,6 +294,14 @@ int lqt_sim_set_state(lqt_sim *s, const double *state_host);
  * form of PlotScript/plot1DECG_compare.py:89-105.  Sampled every `every` steps. */
 int lqt_sim_set_electrodes(lqt_sim *s, int32_t n, const double *xyz_host,
                            int32_t every);
+/* V of every tissue voxel into a host buffer without waiting (the reference
+ * copies V back every step, GPU3D.cu:1802): the gather into one of two device
+ * slots runs on the simulation's stream, the copy on a second stream, so it
+ * overlaps the next steps.  The buffer (pinned memory for a true overlap) is
+ * complete after lqt_sim_wait_v; a buffer must not be reused before that. */
+int lqt_sim_get_v_async(lqt_sim *s, void *v_host, int as_double);
+int lqt_sim_wait_v(lqt_sim *s);
+
 /* Samples recorded since the electrodes were set: [nsamples][n], and time. */
 int lqt_sim_get_ecg(lqt_sim *s, int64_t max_samples, double *phi_host,
                     double *t_host, int64_t *nsamples);

@@ -90,6 +90,11 @@ struct lqt_sim {
     unsigned long long *sur_stats = nullptr;
     int *sur_err = nullptr;
     int64_t sur_launches = 0;
+    // asynchronous V read-back: two device slots, a copy stream, events
+    void *vslot[2] = {nullptr, nullptr};
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t gathered[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
+    int vslot_next = 0;
     // output sampling: tissue mask of the dense grid, lattice buffer
     uint8_t *tmask = nullptr;
     double *samp = nullptr;
@@ -101,6 +106,12 @@ struct lqt_sim {
 
     ~lqt_sim()
     {
+        if (copy_stream) cudaStreamSynchronize(copy_stream);
+        for (int i = 0; i < 2; ++i) {
+            if (gathered[i]) cudaEventDestroy(gathered[i]);
+            if (copied[i]) cudaEventDestroy(copied[i]);
+        }
+        if (copy_stream) cudaStreamDestroy(copy_stream);
         if (graph) cudaGraphExecDestroy(graph);
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
@@ -783,6 +794,47 @@ int lqt_sim_get_v(lqt_sim *s, void *v_host, int as_double)
     }
     CK(cudaMemcpyAsync(v_host, tmp, n * esz, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
+    return LQT_OK;
+}
+
+int lqt_sim_get_v_async(lqt_sim *s, void *v_host, int as_double)
+{
+    if (!s || !v_host) return fail(LQT_ERR_INVALID, "lqt_sim_get_v_async: NULL");
+    const int64_t n = s->ntissue;
+    const size_t esz = as_double ? 8 : 4;
+    if (!s->copy_stream) {
+        if (s->mem.alloc(&s->vslot[0], n * 8) || s->mem.alloc(&s->vslot[1], n * 8)) return LQT_ERR_NOMEM;
+        CK(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
+        for (int i = 0; i < 2; ++i) {
+            CK(cudaEventCreateWithFlags(&s->gathered[i], cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&s->copied[i], cudaEventDisableTiming));
+            CK(cudaEventRecord(s->copied[i], s->copy_stream));
+        }
+    }
+    const int k = s->vslot_next;
+    s->vslot_next ^= 1;
+    void *slot = s->vslot[k];
+    const int32_t *gi = s->dim > 1 ? s->gidx : nullptr;
+    // the slot's previous copy must be done before the gather overwrites it
+    CK(cudaStreamWaitEvent(s->stream, s->copied[k], 0));
+    if (s->fp64()) {
+        if (as_double) CK((launch_gather_v<double, double>((double *)s->vg[s->cur], gi, (double *)slot, n, s->stream)));
+        else CK((launch_gather_v<double, float>((double *)s->vg[s->cur], gi, (float *)slot, n, s->stream)));
+    } else {
+        if (as_double) CK((launch_gather_v<float, double>((float *)s->vg[s->cur], gi, (double *)slot, n, s->stream)));
+        else CK((launch_gather_v<float, float>((float *)s->vg[s->cur], gi, (float *)slot, n, s->stream)));
+    }
+    CK(cudaEventRecord(s->gathered[k], s->stream));
+    CK(cudaStreamWaitEvent(s->copy_stream, s->gathered[k], 0));
+    CK(cudaMemcpyAsync(v_host, slot, n * esz, cudaMemcpyDeviceToHost, s->copy_stream));
+    CK(cudaEventRecord(s->copied[k], s->copy_stream));
+    return LQT_OK;
+}
+
+int lqt_sim_wait_v(lqt_sim *s)
+{
+    if (!s) return fail(LQT_ERR_INVALID, "lqt_sim_wait_v: NULL");
+    if (s->copy_stream) CK(cudaStreamSynchronize(s->copy_stream));
     return LQT_OK;
 }
 

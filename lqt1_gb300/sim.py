@@ -82,6 +82,17 @@ class Sim:
         """V into a caller buffer (float32 or float64, length n)."""
         N.check(N.lib().lqt_sim_get_v(self._h, _p(out), int(out.dtype == np.float64)), "lqt_sim_get_v")
 
+    def get_v_async(self, out: np.ndarray):
+        """Start copying V into `out` (pinned for overlap); complete after wait_v()."""
+        L = N.lib()
+        L.lqt_sim_get_v_async.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        N.check(L.lqt_sim_get_v_async(self._h, _p(out), int(out.dtype == np.float64)), "lqt_sim_get_v_async")
+
+    def wait_v(self):
+        L = N.lib()
+        L.lqt_sim_wait_v.argtypes = [C.c_void_p]
+        N.check(L.lqt_sim_wait_v(self._h), "lqt_sim_wait_v")
+
     def tissue_index(self) -> np.ndarray:
         out = np.zeros(self.n, np.int64)
         N.check(N.lib().lqt_sim_tissue_index(self._h, _p(out)), "lqt_sim_tissue_index")

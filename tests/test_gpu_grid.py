@@ -169,3 +169,28 @@ def test_occupancy_variants_are_bitwise_identical(lq):
     assert np.array_equal(states[0], states[1]) and np.array_equal(states[0], states[2])
     sim.tune(-1)              # the autotuner runs and picks one of them
     assert sim.tune(-1)[0] in (2, 3, 4)
+
+
+@pytest.mark.gpu
+def test_async_v_readback_matches_sync(lq):
+    """lqt_sim_get_v_async: the copies overlap later steps and still deliver
+    the V of the step they were issued after."""
+    import torch
+    sh = lq.geometry.sheet(60, 60, s1_cols=3)
+    sim = lq.Sim(sh.types, 0.15, precision=lq.MIXED, model="lqt1")
+    sim.set_protocol(bcl=1000.0, s1_mask=sh.s1_mask, s1_start=0.0, s1_duration=2.0, s1_strength=-52.0)
+    bufs = [torch.empty(sim.n, dtype=torch.float32, pin_memory=True).numpy() for _ in range(6)]
+    ref = []
+    for i in range(6):
+        sim.step(40)
+        ref.append(sim.get_v())
+        sim.get_v_async(bufs[i])
+    sim.wait_v()
+    for i in range(6):
+        np.testing.assert_array_equal(bufs[i], ref[i])
+    # double precision buffers too
+    b64 = np.zeros(sim.n)
+    sim.step(7)
+    sim.get_v_async(b64)
+    sim.wait_v()
+    np.testing.assert_array_equal(b64, sim.get_v(as_double=True))
