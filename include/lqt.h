@@ -519,7 +519,9 @@ int lqt_sur_prepare(lqt_mlp *m, const float *x_dev, const float *d_dev,
  * passes keeps its new ionic state and, for the next 5 steps, moves V by the
  * macro step's ionic rate plus diffusion only.  Every other voxel runs the
  * plain step.  The network must be trained for this dt (training pairs from
- * lqt_sur_datagen with the same dt).  m = NULL detaches.  m stays owned by
+ * lqt_sur_datagen with the same dt); its inputs carry the model's GKs, PCa and
+ * GKs-ISO factors, so models with ISO gate shifts or a SUPREP dose are
+ * refused.  m = NULL detaches.  m stays owned by
  * the caller and must outlive the attachment; its parameters are read at
  * every macro step. */
 typedef struct lqt_sur_config {

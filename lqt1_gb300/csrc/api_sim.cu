@@ -1093,6 +1093,9 @@ int lqt_sim_set_surrogate(lqt_sim *s, lqt_mlp *m, const lqt_sur_config *cfg)
         return LQT_OK;
     }
     if (s->fp64()) return fail(LQT_ERR_INVALID, "lqt_sim_set_surrogate: the surrogate runs in the mixed form only");
+    if (s->p.model.dss_shift != 0.0 || s->p.model.fss_shift != 0.0 || s->p.model.suprep_dose > 0.0)
+        return fail(LQT_ERR_INVALID, "lqt_sim_set_surrogate: the network's inputs carry the GKs, PCa and GKs-ISO "
+                                     "factors only; models with ISO gate shifts or SUPREP are not covered");
     if (!cfg || !(cfg->dvdt_max > 0) || !(cfg->kappa > 0) || !(cfg->vstep_max > 0) || cfg->reserved != 0 ||
         (cfg->use_net != 0 && cfg->use_net != 1))
         return fail(LQT_ERR_INVALID, "lqt_sim_set_surrogate: dvdt_max, kappa, vstep_max > 0; use_net 0/1; reserved 0");
