@@ -38,10 +38,12 @@ struct DevMem {
         ptrs.push_back(*p);
         return LQT_OK;
     }
-    ~DevMem()
+    void reset()
     {
         for (void *p : ptrs) cudaFree(p);
+        ptrs.clear();
     }
+    ~DevMem() { reset(); }
 };
 
 void initial_state(double v0, double *s);

@@ -79,8 +79,7 @@ static int upload_params(lqt_mlp *m, const std::vector<float> &p)
 static int ensure_ws(lqt_mlp *m, int64_t B)
 {
     if (B <= m->ws_batch) return LQT_OK;
-    m->ws.~DevMem();
-    new (&m->ws) DevMem();
+    m->ws.reset();
     int rc = m->ws.alloc((void **)&m->Z1, B * kMlpHid * 4) | m->ws.alloc((void **)&m->Z2, B * kMlpHid * 4) |
              m->ws.alloc((void **)&m->Y, B * kMlpOut * 4) | m->ws.alloc((void **)&m->H1, B * kMlpHid * 2) |
              m->ws.alloc((void **)&m->H2, B * kMlpHid * 2) | m->ws.alloc((void **)&m->dY, B * kMlpOut * 2) |

@@ -919,7 +919,7 @@ int lqt_sim_set_electrodes(lqt_sim *s, int32_t n, const double *xyz, int32_t eve
     if (!s->el) {
         int rc = s->mem.alloc((void **)&s->el, kMaxElectrodes * sizeof(float4)) |
                  s->mem.alloc((void **)&s->ecg_partial, ecg_blocks(s->ntissue) * kMaxElectrodes * 8) |
-                 s->mem.alloc((void **)&s->ecg_count, 8);
+                 s->mem.alloc((void **)&s->ecg_count, 16);     // samples written, blocks done
         if (rc) return LQT_ERR_NOMEM;
     }
     s->ecg_cap = 1 << 16;
@@ -929,7 +929,7 @@ int lqt_sim_set_electrodes(lqt_sim *s, int32_t n, const double *xyz, int32_t eve
         if (rc) return LQT_ERR_NOMEM;
     }
     CK(cudaMemcpyAsync(s->el, el.data(), n * sizeof(float4), cudaMemcpyHostToDevice, s->stream));
-    CK(cudaMemsetAsync(s->ecg_count, 0, 8, s->stream));
+    CK(cudaMemsetAsync(s->ecg_count, 0, 16, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return LQT_OK;
 }

@@ -293,10 +293,23 @@ __global__ void __launch_bounds__(256) k_ghost(GridDev<R> gd, int nxt)
     }
 }
 
+// Compensated FP32 sum (hi, lo) += x: TwoSum of hi and x, error folded into lo.
+__device__ __forceinline__ void kahan2_add(float &hi, float &lo, float x)
+{
+    const float s = __fadd_rn(hi, x);
+    const float bb = __fsub_rn(s, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+    hi = s;
+    lo = __fadd_rn(lo, e);
+}
+
 // Pseudo-ECG partial sums: 3D form of PlotScript/plot1DECG_compare.py:89-105,
 // phi(r0) = sum_i sum_axis (V[i+e] - V[i-e])/2 (r_i - r0)_axis / |r_i - r0|^3.
-// One FP64 partial per block and electrode, reduced in a fixed order by
-// k_ecg_final so the result does not depend on scheduling.
+// Warps sum their 32 FP32 terms as compensated FP32 pairs (a fixed shuffle
+// tree; FP64 arithmetic runs at a small fraction of the FP32 rate on this
+// GPU), the block's warp sums are added in FP64, and k_ecg_final adds the
+// per-block partials in a fixed order, so the result does not depend on
+// scheduling.
 template <typename R, int DIM>
 __global__ void __launch_bounds__(256) k_ecg_partial(GridDev<R> gd, const R *__restrict__ V,
                                                      const float4 *__restrict__ el, int nel,
@@ -315,8 +328,10 @@ __global__ void __launch_bounds__(256) k_ecg_partial(GridDev<R> gd, const R *__r
             const int64_t n = gd.ntissue;
             if (n > 1) h[0] = k == 0 ? (float)(V[1] - V[0]) : (k == n - 1 ? (float)(V[k] - V[k - 1]) : 0.5f * (float)(V[k + 1] - V[k - 1]));
         } else {
-            const int64_t x = g / gd.sx, rem = g - x * gd.sx;
-            const int64_t y = rem / gd.sy, z = rem - y * gd.sy;
+            // grids are below 2^31 voxels: 32-bit index arithmetic
+            const int32_t g32 = (int32_t)g, sx32 = (int32_t)gd.sx, sy32 = (int32_t)gd.sy;
+            const int32_t x = g32 / sx32, rem = g32 - x * sx32;
+            const int32_t y = rem / sy32, z = rem - y * sy32;
             p[0] = (float)((x - gd.pad) * gd.dx);
             p[1] = (float)((y - gd.pad) * gd.dx);
             p[2] = (float)((DIM == 3 ? z - gd.pad : 0) * gd.dx);
@@ -338,9 +353,14 @@ __global__ void __launch_bounds__(256) k_ecg_partial(GridDev<R> gd, const R *__r
 #pragma unroll
     for (int e = 0; e < kMaxElectrodes; ++e) {
         if (e >= nel) break;
-        double v = (double)acc[e];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) red[wid][e] = v;
+        float hi = acc[e], lo = 0.f;
+        for (int o = 16; o > 0; o >>= 1) {
+            const float oh = __shfl_down_sync(0xffffffffu, hi, o);
+            const float ol = __shfl_down_sync(0xffffffffu, lo, o);
+            kahan2_add(hi, lo, oh);
+            lo = __fadd_rn(lo, ol);
+        }
+        if (lane == 0) red[wid][e] = (double)hi + (double)lo;
     }
     __syncthreads();
     if (threadIdx.x < nel) {

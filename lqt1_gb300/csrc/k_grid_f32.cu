@@ -31,36 +31,42 @@ cudaError_t launch_ecg<float>(const GridDev<float> &gd, int cur, const float4 *e
     if (dim == 1) k_ecg_partial<float, 1><<<(unsigned)nb, 256, 0, st>>>(gd, gd.vg[cur], el, nel, partial);
     else if (dim == 2) k_ecg_partial<float, 2><<<(unsigned)nb, 256, 0, st>>>(gd, gd.vg[cur], el, nel, partial);
     else k_ecg_partial<float, 3><<<(unsigned)nb, 256, 0, st>>>(gd, gd.vg[cur], el, nel, partial);
-    k_ecg_final<<<1, 256, 0, st>>>(partial, nb, nel, out, t_out, counter, cap, gd.clk);
+    k_ecg_final<<<nel, 256, 0, st>>>(partial, nb, nel, out, t_out, counter, cap, gd.clk);
     return cudaGetLastError();
 }
 
 int64_t ecg_blocks(int64_t ntissue) { return ntissue <= 0 ? 1 : (ntissue + 255) / 256; }
 
-// Sum the per-block partials of each electrode in block order (deterministic).
+// Sum the per-block partials of each electrode in block order (deterministic):
+// one block per electrode; the last block to finish (a counter in the same
+// launch) records the time and advances the sample counter.
 __global__ void k_ecg_final(const double *__restrict__ partial, int64_t nblocks, int nel, double *__restrict__ out,
                             double *__restrict__ t_out, int64_t *__restrict__ counter, int64_t cap,
                             const Clock *__restrict__ clk)
 {
     __shared__ double red[256];
-    const int64_t slot = *counter;
+    const int64_t slot = counter[0];
     if (slot >= cap) return;
-    out += slot * nel;
-    for (int e = 0; e < nel; ++e) {
-        double s = 0.0;
-        for (int64_t b = threadIdx.x; b < nblocks; b += blockDim.x) s += partial[b * nel + e];
-        red[threadIdx.x] = s;
-        __syncthreads();
-        for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-            if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) out[e] = red[0];
+    const int e = blockIdx.x;
+    double s = 0.0;
+    for (int64_t b = threadIdx.x; b < nblocks; b += blockDim.x) s += partial[b * nel + e];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        t_out[slot] = clk->time;
-        *counter = slot + 1;
+        out[slot * nel + e] = red[0];
+        __threadfence();
+        // counter[1]: blocks of this sample done
+        const unsigned long long done = atomicAdd(reinterpret_cast<unsigned long long *>(counter + 1), 1ull) + 1;
+        if (done == (unsigned long long)nel) {
+            t_out[slot] = clk->time;
+            counter[1] = 0;
+            __threadfence();
+            counter[0] = slot + 1;
+        }
     }
 }
 

@@ -43,7 +43,7 @@ cudaError_t launch_ecg<double>(const GridDev<double> &gd, int cur, const float4 
     if (dim == 1) k_ecg_partial<double, 1><<<(unsigned)nb, 256, 0, st>>>(gd, gd.vg[cur], el, nel, partial);
     else if (dim == 2) k_ecg_partial<double, 2><<<(unsigned)nb, 256, 0, st>>>(gd, gd.vg[cur], el, nel, partial);
     else k_ecg_partial<double, 3><<<(unsigned)nb, 256, 0, st>>>(gd, gd.vg[cur], el, nel, partial);
-    k_ecg_final<<<1, 256, 0, st>>>(partial, nb, nel, out, t_out, counter, cap, gd.clk);
+    k_ecg_final<<<nel, 256, 0, st>>>(partial, nb, nel, out, t_out, counter, cap, gd.clk);
     return cudaGetLastError();
 }
 

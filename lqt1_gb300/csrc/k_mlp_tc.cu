@@ -165,12 +165,9 @@ cudaError_t launch_mlp_infer_tc(const __nv_bfloat16 *X, float *Y, const MlpDev &
                                 cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    static std::atomic<uint64_t> attr_done{0};
+    cudaError_t e = tc::smem_attr_once(k_mlp_infer_tc, kSmemBytes, attr_done);
+    if (e != cudaSuccess) return e;
     int dev = 0, nsm = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);

@@ -498,12 +498,9 @@ uint32_t sur_grid_smem_bytes() { return kSmemBytes; }
 cudaError_t launch_sur_grid(const GridDev<float> &gd, const SurGrid &sg, int cur, int dim, cudaStream_t st)
 {
     if (gd.ntissue <= 0) return cudaSuccess;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_sur_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    static std::atomic<uint64_t> attr_done{0};
+    cudaError_t e = tc::smem_attr_once(k_sur_grid, kSmemBytes, attr_done);
+    if (e != cudaSuccess) return e;
     int dev = 0, nsm = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);

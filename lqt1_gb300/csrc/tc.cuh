@@ -11,8 +11,25 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 namespace lqt {
 namespace tc {
+
+// Opt a kernel into more than 48 KB of dynamic shared memory once per device
+// (the attribute belongs to the device's context); `done` is the launcher's
+// own bit set of devices.
+template <typename K> inline cudaError_t smem_attr_once(K kernel, uint32_t bytes, std::atomic<uint64_t> &done)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const uint64_t bit = dev < 64 ? (1ull << dev) : 0;
+    if (bit && (done.load() & bit)) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess && bit) done.fetch_or(bit);
+    return e;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p)
 {
