@@ -203,6 +203,8 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=10)
     ap.add_argument("--mixed-steps", type=int, default=-1, help="steps of the plain mixed leg (-1 = --steps)")
     ap.add_argument("--no-accuracy", dest="accuracy", action="store_false")
+    ap.add_argument("--no-configs", dest="configs", action="store_false",
+                    help="skip the config 1 (OneD strand) and config 2 (2D sheet) legs")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sweep-beats", type=int, default=2,
                     help="beats of the 4096-instance batched sweep leg (0 = skip; 20 = the full sweep)")
@@ -371,6 +373,11 @@ def main():
     if args.accuracy:
         accuracy = accuracy_leg(lq, net, stream)
 
+    # ---- the other configurations of the reference's drivers -----------------
+    configs = None
+    if args.configs:
+        configs = {"config1_oned_strand": config1_leg(lq), "config2_sheet2d": config2_leg(lq, net, stream)}
+
     # batched sweep leg: 4096 uneven single cells / strands (50-400 cells), own
     # parameters each, one persistent graph-captured launch (autotuned shape)
     sweep = None
@@ -420,9 +427,62 @@ def main():
                        "step_kernel_variant": {"min_ctas_per_sm": variant,
                                                "tuned_ms": [round(float(x), 4) for x in tune_ms[:3]]}},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "surrogate": surrogate, "mixed_form": mixed,
-            "fp64_form": fp64, "accuracy": accuracy, "batched_sweep": sweep, "gpu_launches": launches,
+            "fp64_form": fp64, "accuracy": accuracy, "batched_sweep": sweep, "other_configs": configs,
+            "gpu_launches": launches,
             "clocks": clocks, "blowup_voxel_steps": nbad}
     print(json.dumps(line), flush=True)
+
+
+def config1_leg(lq):
+    """OneD.cc: 100 cells, 5 beats + 1 cycle (6 s), one persistent launch;
+    launch-latency bound by construction (2.5e7 cell-steps)."""
+    out = {"workload": "OneD.cc strand, 100 cells, 6000 ms, V every 10 steps"}
+    # FP64: one strand is one CTA on one SM at the FP64 rate; a 500 ms sample
+    for name, prec, t_ms in (("fp64", lq.FP64, 500.0), ("mixed", lq.MIXED, 6000.0)):
+        st = lq.OneDStrand(model="default", precision=prec, num_s1=5 if t_ms >= 6000.0 else 0, stop_time=t_ms)
+        r = st.run()
+        work = 100 * round(t_ms / 0.02)
+        out[name] = {"device_ms": r["device_ms"], "cell_steps_per_s": work / (r["device_ms"] / 1e3),
+                     "simulated_ms": t_ms}
+        if prec == lq.MIXED:
+            out[name]["cv_m_per_s"] = float(r["cv"])
+    return out
+
+
+def config2_leg(lq, net, stream):
+    """The 600 x 600 sheet at 0.15 mm, S1 line at x = 0, S2 quadrant at a
+    seeded coupling interval U[300, 360] ms, 2 s: mixed and FP32 + surrogate."""
+    import torch
+    rng = np.random.default_rng(7)
+    ci = float(rng.uniform(300.0, 360.0))
+    sh = lq.geometry.sheet(600, 600)
+    m = lq.model("lqt1", gks_scale=0.5)
+    out = {"workload": "2d-sheet 600x600 @0.15mm, S1 + S2 at %.1f ms, 2000 ms" % ci,
+           "note": "the -104 pA/pF S2 over a whole quadrant lifts V to about 284 mV inside it (FP64 and mixed "
+                   "alike); the blow-up count here is NaN/overflow only"}
+    nsteps = 100000
+    for name, sur in (("mixed", False), ("surrogate", True)):
+        sim = lq.Sim(sh.types, 0.15, precision=lq.MIXED, model=m, stream=stream.cuda_stream, vmin_ok=-1e9,
+                     vmax_ok=1e9)
+        sim.set_protocol(bcl=1000.0, s1_mask=sh.s1_mask, s1_start=0.0, s1_duration=2.0, s1_strength=-52.0,
+                         s1_beats=1, s2_time=ci, s2_duration=3.0, s2_strength=-104.0, s2_mask=sh.s2_mask)
+        if sur:
+            sim.set_surrogate(net)
+        sim.step(100)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        sim.step(nsteps - 100)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        out[name] = {"cell_steps_per_s": sim.n * (nsteps - 100) / (ms / 1e3), "device_ms": ms,
+                     "blowup_voxel_steps": sim.check()}
+        if sur:
+            st = sim.surrogate_stats()
+            out[name]["accepted_frac_of_voxel_macro_steps"] = st["accepted"] / max(1, st["macro_steps"] * sim.n)
+        sim.close()
+    return out
 
 
 def accuracy_leg(lq, net, stream):
