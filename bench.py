@@ -9,7 +9,7 @@ Default: 3D truncated prolate-ellipsoid shell in a 320x320x420 grid at
 0.2 mm (about 7.1M tissue voxels), fibres +60 -> -60 degrees, IKs x0.5,
 beta-adrenergic ICaL x2 / IKs x1.5, apical stimulus at BCL 800 ms, timed over
 one whole beat (40000 steps).  The headline form is FP32 + learned surrogate
-(0.1 ms macro steps of a coarse TPORd step plus a BF16 tensor-core network's
+(0.2 ms macro steps of a coarse TPORd step plus a BF16 tensor-core network's
 correction where |dV/dt| <= 1 mV/ms; plain steps elsewhere).  Beside it: the
 plain mixed form over the same steps, the plain FP64 form, the APD90 /
 activation error of both FP32 forms against FP64 on a 100k-voxel shell over a
@@ -51,6 +51,9 @@ BYTES_FP64 = 8 * 8 * 2 + 29 * 8 * 2 + 8 + 8 + 4 + 1 + 9 * 8 + 16
 BYTES_SUR_MACRO = 4 + 4 + 4 + 1 + 16 + (8 * 8 + 29 * 4) * 2 + 4
 # and the network's multiply-adds (48 -> 128 -> 128 -> 48) per voxel
 FLOP_SUR_MACRO = 2 * (48 * 128 + 128 * 128 + 128 * 48)
+# surrogate acceptance thresholds passed to every set_surrogate call (set
+# from the command line in main)
+SUR_CFG = {}
 
 
 def workload_model():
@@ -200,6 +203,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ventricle3d", choices=["ventricle3d", "ventricle3d_small", "sheet2d"])
     ap.add_argument("--prerun", type=int, default=0, help="untimed steps before the timed region (setup)")
+    ap.add_argument("--weights", default=None, help="surrogate network file (default: the shipped network)")
+    ap.add_argument("--sur-dvdt-max", type=float, default=1.0, help="surrogate eligibility: |dV/dt| bound, mV/ms")
+    ap.add_argument("--sur-vstep-max", type=float, default=0.3, help="surrogate residual check: ionic dV per macro step")
     ap.add_argument("--fp64-steps", type=int, default=10)
     ap.add_argument("--mixed-steps", type=int, default=-1, help="steps of the plain mixed leg (-1 = --steps)")
     ap.add_argument("--no-accuracy", dest="accuracy", action="store_false")
@@ -244,7 +250,8 @@ def main():
     dev = torch.cuda.current_device()
     w = build_workload(args.workload)
     stream = torch.cuda.Stream()
-    net = S.load(stream=stream.cuda_stream)
+    net = S.load(args.weights, stream=stream.cuda_stream)
+    SUR_CFG.update(dvdt_max=args.sur_dvdt_max, vstep_max=args.sur_vstep_max)
 
     def make_sim(precision, surrogate):
         sim = lq.Sim(w["types"], w["dx"], fibre=w["fibre"], precision=precision, model=workload_model(),
@@ -253,7 +260,7 @@ def main():
                          s1_beats=3, s2_time=-1.0)
         sim.set_electrodes(np.array(w["electrodes"]), every=50)
         if surrogate:
-            sim.set_surrogate(net)
+            sim.set_surrogate(net, **SUR_CFG)
         return sim
 
     def barrier():
@@ -292,7 +299,7 @@ def main():
     peak = peak or 6800.0
     tpeak = peaks.get("bf16_tflops_sustained") or peaks.get("bf16_tflops") or 1700.0
     # dominant kernel of the surrogate form: the macro-step kernel (one launch
-    # per 5 steps), algorithmic bytes and tensor FLOPs per voxel per launch
+    # per macro step), algorithmic bytes and tensor FLOPs per voxel per launch
     ach_sur = BYTES_SUR_MACRO * n / (ms_sur / 1e3) / 1e9
     roof = {"bound": "hbm", "achieved": ach_sur, "peak": peak, "unit": "GB/s", "frac": ach_sur / peak,
             "traffic": traffic_summary("k_sur_grid_ventricle3d.json"), "kernel": "k_sur_grid", "kernel_ms": ms_sur,
@@ -409,16 +416,18 @@ def main():
                          f"OpenMP on {r['cores']} threads, {cpu_model_name()}"}
     clocks = clk.summary()
     # our kernels in the timed region: per step the V-only substep, the plain
-    # step over the listed voxels and the ghost/clock kernel; per 5 steps the
-    # macro-step kernel; per 50 steps the two ECG kernels
-    launches = 3 * args.steps + args.steps // 5 + 2 * (args.steps // 50)
+    # step over the listed voxels and the ghost/clock kernel; per macro step
+    # (net.nsub steps) the macro-step kernel; per 50 steps the two ECG kernels
+    launches = 3 * args.steps + sst["macro_steps"] + 2 * (args.steps // 50)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": w["desc"], "tissue_voxels": n,
                        "form": "FP32 + learned surrogate (FP32 gates/currents/diffusion, Kahan-compensated FP32 "
-                               "concentrations; 0.1 ms macro steps of a coarse TPORd step + BF16 tcgen05 MLP "
-                               "correction where |dV/dt| <= 1 mV/ms, plain 0.02 ms steps elsewhere)",
+                               "concentrations; %g ms macro steps of a coarse TPORd step + BF16 tcgen05 MLP "
+                               "correction where |dV/dt| <= %g mV/ms, plain 0.02 ms steps elsewhere)"
+                               % (round(0.02 * net.nsub, 3), args.sur_dvdt_max),
+                       "surrogate_thresholds": dict(SUR_CFG),
                        "dt_ms": 0.02, "t_ms": [round((args.prerun + args.warmup + 15) * 0.02, 2),
                                                round((args.prerun + args.warmup + 15 + args.steps) * 0.02, 2)],
                        "electrodes": len(w["electrodes"]),
@@ -467,7 +476,7 @@ def config2_leg(lq, net, stream):
         sim.set_protocol(bcl=1000.0, s1_mask=sh.s1_mask, s1_start=0.0, s1_duration=2.0, s1_strength=-52.0,
                          s1_beats=1, s2_time=ci, s2_duration=3.0, s2_strength=-104.0, s2_mask=sh.s2_mask)
         if sur:
-            sim.set_surrogate(net)
+            sim.set_surrogate(net, **SUR_CFG)
         sim.step(100)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
@@ -499,7 +508,7 @@ def accuracy_leg(lq, net, stream):
         sim.set_protocol(bcl=800.0, s1_mask=v.s1_mask, s1_start=0.0, s1_duration=2.0, s1_strength=-52.0,
                          s1_beats=1)
         if sur:
-            sim.set_surrogate(net)
+            sim.set_surrogate(net, **SUR_CFG)
         sim.step(nsteps)
         res[name] = sim.detect()
         sim.close()

@@ -484,12 +484,12 @@ int lqt_mlp_train_step(lqt_mlp *m, const void *x_bf16_dev, const float *t_dev,
  * ncells paced cells with seeded uniform parameters in the given ranges
  * (GKs factor, PCa factor, GKs-ISO factor, BCL; type uniform over
  * endo/M/epi; 2 ms x -52 pA/pF at 50 ms of each cycle).  After beats_warm
- * cycles, at macro-step boundaries where |dV/dt| <= dvdt_max and no stimulus
- * falls in the next 0.1 ms, each cell records with probability prob:
- * x_dev[row][44] = 38 states (V, 8 concentrations, 29 gates) + 3 factors +
- * endo/epi/M one-hot, d_dev[row][38] = the state after 5 plain steps of
- * 0.02 ms minus the state after one coarse step of 0.1 ms from the same
- * start (the correction the network learns).  Macro steps that are not
+ * cycles, at macro-step boundaries (every nsub steps) where |dV/dt| <=
+ * dvdt_max and no stimulus falls in the coming macro step, each cell records
+ * with probability prob: x_dev[row][44] = 38 states (V, 8 concentrations, 29
+ * gates) + 3 factors + endo/epi/M one-hot, d_dev[row][38] = the state after
+ * nsub plain steps of dt minus the state after one coarse step of nsub * dt
+ * from the same start (the correction the network learns).  Macro steps that are not
  * recorded carry a seeded constant current uniform in +-jitter pA/pF, which
  * moves the cells off the single-cell trajectory as tissue coupling does.
  * Up to cap rows; *count = rows written. */
@@ -497,6 +497,8 @@ typedef struct lqt_sur_ranges {
     double gks[2], pca[2], iso[2], bcl[2];
     int32_t beats_warm, beats_record;
     double dt, dvdt_max, prob, jitter;
+    int32_t nsub;       /* plain steps per macro step; divides 50; 0 = 5 */
+    int32_t reserved;   /* must be zero */
 } lqt_sur_ranges;
 int lqt_sur_datagen(int64_t ncells, uint64_t seed, const lqt_sur_ranges *ranges,
                     float *x_dev, float *d_dev, int64_t cap, int64_t *count,
@@ -507,19 +509,19 @@ int lqt_sur_datagen(int64_t ncells, uint64_t seed, const lqt_sur_ranges *ranges,
 int lqt_sur_prepare(lqt_mlp *m, const float *x_dev, const float *d_dev,
                     const int64_t *idx_dev, int64_t n, void *xb_dev, float *t_dev);
 
-/* The surrogate inside a tissue simulation (mixed form only).  Every 5
- * steps (steps whose index is a multiple of 5) one kernel offers each tissue
- * voxel whose |dV/dt| over the last step is at most dvdt_max, and that no
- * stimulus reaches in the next 5 steps, to the surrogate: one coarse TPORd
- * step of 5 dt plus the network's correction (use_net = 1; 0 = the coarse
- * step alone).  The residual check (every normalised correction within
+/* The surrogate inside a tissue simulation (mixed form only).  Every nsub
+ * steps (steps whose index is a multiple of nsub; nsub divides 50, 0 = 5)
+ * one kernel offers each tissue voxel whose |dV/dt| over the last step is at
+ * most dvdt_max, and that no stimulus reaches in the next nsub steps, to the
+ * surrogate: one coarse TPORd step of nsub * dt plus the network's
+ * correction (use_net = 1; 0 = the coarse step alone).  The residual check (every normalised correction within
  * +-kappa times its bound, lqt_mlp_set_bounds; gates within [0, 1];
  * concentrations positive; ionic V change of the macro step within
  * +-vstep_max mV) decides per voxel; a voxel that
- * passes keeps its new ionic state and, for the next 5 steps, moves V by the
+ * passes keeps its new ionic state and, for the next nsub steps, moves V by the
  * macro step's ionic rate plus diffusion only.  Every other voxel runs the
- * plain step.  The network must be trained for this dt (training pairs from
- * lqt_sur_datagen with the same dt); its inputs carry the model's GKs, PCa and
+ * plain step.  The network must be trained for this dt and nsub (training
+ * pairs from lqt_sur_datagen with the same dt and nsub); its inputs carry the model's GKs, PCa and
  * GKs-ISO factors, so models with ISO gate shifts or a SUPREP dose are
  * refused.  m = NULL detaches.  m stays owned by
  * the caller and must outlive the attachment; its parameters are read at
@@ -529,7 +531,7 @@ typedef struct lqt_sur_config {
     double kappa;       /* multiplier of the network's residual bounds, e.g. 1.5 */
     double vstep_max;   /* mV per macro step, e.g. 0.3 */
     int32_t use_net;
-    int32_t reserved;   /* must be zero */
+    int32_t nsub;       /* plain steps per macro step; divides 50; 0 = 5 */
 } lqt_sur_config;
 int lqt_sim_set_surrogate(lqt_sim *s, lqt_mlp *m, const lqt_sur_config *cfg);
 /* Counters since the last reset: macro steps launched, voxel offers, voxels

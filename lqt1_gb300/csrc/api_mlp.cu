@@ -295,6 +295,9 @@ int lqt_sur_datagen(int64_t ncells, uint64_t seed, const lqt_sur_ranges *r, floa
     if (!(r->bcl[0] > 10) || r->bcl[1] < r->bcl[0] || r->beats_warm < 0 || r->beats_record < 1 || !(r->dt > 0) ||
         !(r->prob > 0) || r->prob > 1 || !(r->jitter >= 0))
         return fail(LQT_ERR_INVALID, "lqt_sur_datagen: ranges (bcl > 10, beats_record >= 1, 0 < prob <= 1, dt > 0, jitter >= 0)");
+    const int nsub = sur_nsub_or_default(r->nsub);
+    if (!sur_nsub_ok(nsub) || r->reserved != 0)
+        return fail(LQT_ERR_INVALID, "lqt_sur_datagen: nsub must divide 50 (0 = 5); reserved must be zero");
     std::mt19937_64 rng(seed);
     std::uniform_real_distribution<double> U(0.0, 1.0);
     std::vector<SurCell> cells(ncells);
@@ -331,8 +334,8 @@ int lqt_sur_datagen(int64_t ncells, uint64_t seed, const lqt_sur_ranges *r, floa
     CK(cudaMemcpyAsync(dc, cells.data(), ncells * sizeof(SurCell), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(dm, models.data(), ncells * sizeof(ModelK), cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(cnt, 0, 8, st));
-    CK(launch_sur_datagen(dc, ncells, dm, make_stepk(r->dt), make_stepk(kSurSteps * r->dt), x_dev, d_dev, cnt, cap,
-                          seed, (float)r->dvdt_max, (float)r->prob, (float)r->jitter, st));
+    CK(launch_sur_datagen(dc, ncells, dm, make_stepk(r->dt), make_stepk(nsub * r->dt), x_dev, d_dev, cnt, cap,
+                          seed, (float)r->dvdt_max, (float)r->prob, (float)r->jitter, nsub, st));
     unsigned long long c = 0;
     CK(cudaMemcpyAsync(&c, cnt, 8, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));

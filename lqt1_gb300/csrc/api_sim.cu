@@ -30,7 +30,7 @@ using namespace lqt;
 namespace {
 constexpr int kGraphChunk = 50;   // steps per captured graph (even: V buffer parity is kept;
                                   // a multiple of the surrogate's macro step)
-static_assert(kGraphChunk % kSurSteps == 0, "graph chunks must start on macro-step boundaries");
+static_assert(kGraphChunk == kSurSpan, "graph chunks must start on macro-step boundaries");
 constexpr uint32_t kCkptMagic = 0x4c515443;   // "LQTC"
 constexpr uint32_t kCkptVersion = 1;
 }  // namespace
@@ -82,6 +82,7 @@ struct lqt_sim {
     // learned surrogate (mixed form): network, per-voxel rate, counters
     lqt_mlp *sur = nullptr;
     lqt_sur_config sur_cfg{};
+    int sur_nsub = kSurSteps;       // plain steps per macro step
     float *srate = nullptr;
     uint8_t *sdflag = nullptr;
     int32_t *plist = nullptr;
@@ -241,7 +242,7 @@ int refresh_windows(lqt_sim *s, int64_t horizon)
 // At a macro-step boundary with a surrogate attached: the macro-step kernel.
 int launch_sur_if_due(lqt_sim *s)
 {
-    if (!s->sur || s->step % kSurSteps != 0) return LQT_OK;
+    if (!s->sur || s->step % s->sur_nsub != 0) return LQT_OK;
     SurGrid sg{};
     if (!mlp_device_view(s->sur, &sg.w, &sg.norm)) return fail(LQT_ERR_STATE, "surrogate network has no parameters");
     sg.rate = s->srate;
@@ -250,14 +251,14 @@ int launch_sur_if_due(lqt_sim *s)
     sg.plist_n = s->plist_n;
     sg.stats = s->sur_stats;
     sg.err = s->sur_err;
-    sg.kmac = step_as<float>(make_stepk(kSurSteps * s->p.dt));
+    sg.kmac = step_as<float>(make_stepk(s->sur_nsub * s->p.dt));
     sg.par[0] = (float)s->p.model.gks_scale;
     sg.par[1] = (float)s->p.model.pca_scale;
     sg.par[2] = (float)s->p.model.gks_iso_scale;
     sg.dvdt_max = (float)s->sur_cfg.dvdt_max;
     sg.kappa = (float)s->sur_cfg.kappa;
     sg.vstep_max = (float)s->sur_cfg.vstep_max;
-    sg.nsub = kSurSteps;
+    sg.nsub = s->sur_nsub;
     sg.use_net = s->sur_cfg.use_net;
     CK(cudaMemsetAsync(s->plist_n, 0, sizeof(unsigned long long), s->stream));
     CK(launch_sur_grid(devf<float>(s), sg, s->cur, s->dim, s->stream));
@@ -758,7 +759,7 @@ int lqt_sim_step(lqt_sim *s, int64_t nsteps)
             }
             CK(cudaGraphLaunch(s->graph, s->stream));
             if (s->sur) {
-                s->sur_launches += kGraphChunk / kSurSteps;   // chunks start on macro-step boundaries
+                s->sur_launches += kGraphChunk / s->sur_nsub;   // chunks start on macro-step boundaries
                 s->plist_valid = true;
             }
             s->step += kGraphChunk;
@@ -1004,7 +1005,7 @@ int lqt_sim_profile(lqt_sim *s, int64_t nsteps, double *ms_step, double *ms_ghos
     int64_t n_sur = 0;
     int rc = LQT_OK;
     for (int64_t i = 0; i < nsteps && rc == LQT_OK; ++i) {
-        if (s->sur && s->step % kSurSteps == 0) {
+        if (s->sur && s->step % s->sur_nsub == 0) {
             cudaError_t e = cudaEventRecord(ev[3], s->stream);
             if (e == cudaSuccess) rc = launch_sur_if_due(s);
             if (e == cudaSuccess && rc == LQT_OK) e = cudaEventRecord(ev[4], s->stream);
@@ -1096,9 +1097,10 @@ int lqt_sim_set_surrogate(lqt_sim *s, lqt_mlp *m, const lqt_sur_config *cfg)
     if (s->p.model.dss_shift != 0.0 || s->p.model.fss_shift != 0.0 || s->p.model.suprep_dose > 0.0)
         return fail(LQT_ERR_INVALID, "lqt_sim_set_surrogate: the network's inputs carry the GKs, PCa and GKs-ISO "
                                      "factors only; models with ISO gate shifts or SUPREP are not covered");
-    if (!cfg || !(cfg->dvdt_max > 0) || !(cfg->kappa > 0) || !(cfg->vstep_max > 0) || cfg->reserved != 0 ||
-        (cfg->use_net != 0 && cfg->use_net != 1))
-        return fail(LQT_ERR_INVALID, "lqt_sim_set_surrogate: dvdt_max, kappa, vstep_max > 0; use_net 0/1; reserved 0");
+    if (!cfg || !(cfg->dvdt_max > 0) || !(cfg->kappa > 0) || !(cfg->vstep_max > 0) ||
+        !sur_nsub_ok(sur_nsub_or_default(cfg->nsub)) || (cfg->use_net != 0 && cfg->use_net != 1))
+        return fail(LQT_ERR_INVALID, "lqt_sim_set_surrogate: dvdt_max, kappa, vstep_max > 0; use_net 0/1; "
+                                     "nsub divides 50 (0 = 5)");
     MlpDev w;
     const float *nrm = nullptr;
     if (!mlp_device_view(m, &w, &nrm)) return fail(LQT_ERR_INVALID, "lqt_sim_set_surrogate: network not initialised");
@@ -1118,6 +1120,7 @@ int lqt_sim_set_surrogate(lqt_sim *s, lqt_mlp *m, const lqt_sur_config *cfg)
     CK(cudaStreamSynchronize(s->stream));
     s->sur = m;
     s->sur_cfg = *cfg;
+    s->sur_nsub = sur_nsub_or_default(cfg->nsub);
     s->plist_valid = false;
     s->graph_valid = false;
     return LQT_OK;

@@ -1,9 +1,9 @@
 // k_sur.cu -- the learned surrogate around the plain integrator:
 //   * training pairs generated by the plain mixed-form TPORd step,
 //   * feature normalisation into the network's BF16 inputs.
-// A surrogate macro step advances a cell by kSurSteps plain steps (0.1 ms at
-// dt = 0.02 ms) with no diffusion and no stimulus: one coarse TPORd step of
-// 0.1 ms plus the network's correction of the 38 evolving states.
+// A surrogate macro step advances a cell by nsub plain steps (nsub = 5: 0.1 ms
+// at dt = 0.02 ms) with no diffusion and no stimulus: one coarse TPORd step of
+// the macro length plus the network's correction of the 38 evolving states.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -31,7 +31,7 @@ __device__ __forceinline__ void sur_init_cell(CellState<float> &c)
 // One thread per cell: pace with the plain mixed step, and at macro-step
 // boundaries in the surrogate's regime (|dV/dt| <= dvdt_max, no stimulus in
 // the coming macro step, past the warm-up) record, with probability `prob`,
-// the inputs and the correction: state after kSurSteps plain steps minus the
+// the inputs and the correction: state after nsub plain steps minus the
 // state after one coarse step of the macro length from the same start.
 // Macro steps that are not recorded carry a constant current uniform in
 // +-jitter (a stand-in for the electrotonic load of tissue).
@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(128) k_sur_datagen(const SurCell *__restrict__
                                                      StepT<float> kmac, float *__restrict__ X,
                                                      float *__restrict__ D, unsigned long long *__restrict__ counter,
                                                      int64_t cap, uint64_t seed, float dvdt_max, float prob,
-                                                     float jitter)
+                                                     float jitter, int nsub)
 {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= ncells) return;
@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(128) k_sur_datagen(const SurCell *__restrict__
     float ipert = 0.f;
     for (int64_t st = 0; st < sc.nsteps; ++st) {
         const int64_t ph = st % sc.bcl_steps;
-        if (st % kSurSteps == 0) {
+        if (st % nsub == 0) {
             if (slot >= 0) {
                 // finish the pending sample: fine minus coarse
                 float x1[kMlpNState];
@@ -72,9 +72,9 @@ __global__ void __launch_bounds__(128) k_sur_datagen(const SurCell *__restrict__
                 for (int j = 9; j < kMlpNState; ++j) d[j] = x1[j] - xc[j];
                 slot = -1;
             }
-            const bool stim_ahead = ph + kSurSteps > sc.stim_on && ph < sc.stim_off;
+            const bool stim_ahead = ph + nsub > sc.stim_on && ph < sc.stim_off;
             ipert = 0.f;
-            if (st >= sc.warm_steps && !stim_ahead && fabsf(o.dvdt) <= dvdt_max && st + kSurSteps <= sc.nsteps &&
+            if (st >= sc.warm_steps && !stim_ahead && fabsf(o.dvdt) <= dvdt_max && st + nsub <= sc.nsteps &&
                 (sur_hash(seed, (uint64_t)i, (uint64_t)st) & 0xFFFFFF) < (uint32_t)(prob * 16777216.f)) {
                 const unsigned long long s = atomicAdd(counter, 1ull);
                 if (s < (unsigned long long)cap) {
@@ -131,12 +131,12 @@ __global__ void k_sur_prepare(const float *__restrict__ X, const float *__restri
 
 cudaError_t launch_sur_datagen(const SurCell *cells, int64_t ncells, const ModelK *models, const StepK &k,
                                const StepK &kmac, float *X, float *D, unsigned long long *counter, int64_t cap,
-                               uint64_t seed, float dvdt_max, float prob, float jitter, cudaStream_t st)
+                               uint64_t seed, float dvdt_max, float prob, float jitter, int nsub, cudaStream_t st)
 {
     if (ncells <= 0) return cudaSuccess;
     k_sur_datagen<<<(unsigned)((ncells + 127) / 128), 128, 0, st>>>(cells, ncells, models, step_as<float>(k),
                                                                     step_as<float>(kmac), X, D, counter, cap, seed,
-                                                                    dvdt_max, prob, jitter);
+                                                                    dvdt_max, prob, jitter, nsub);
     return cudaGetLastError();
 }
 

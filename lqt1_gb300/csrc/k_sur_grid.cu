@@ -1,6 +1,6 @@
 // k_sur_grid.cu -- the learned surrogate's macro step on a tissue grid.
 //
-// At every macro-step boundary (every kSurSteps plain steps) one persistent
+// At every macro-step boundary (every nsub plain steps) one persistent
 // kernel walks the tissue voxels in tiles of 128.  A voxel is offered to the
 // surrogate when |dV/dt| over the last plain step (both V buffers are still
 // resident) is at most dvdt_max, no stimulus reaches it during the macro step
@@ -15,15 +15,15 @@
 //      accumulators back with tcgen05.ld, apply SiLU and write the next FP16
 //      operand into shared memory);
 //   3. each thread reloads its state, advances it by one coarse TPORd step of
-//      the macro length (dt = kSurSteps * dt, no diffusion) and adds the
-//      network's output, the correction to the state after kSurSteps plain
+//      the macro length (dt = nsub * dt, no diffusion) and adds the
+//      network's output, the correction to the state after nsub plain
 //      steps, read from TMEM.
 // Residual check: every normalised correction within +-kappa times its bound
 // (the largest correction of the training set: the network is not
 // extrapolating), gates within [0, 1] up to a small tolerance (then clamped),
 // concentrations positive, and the macro step's ionic V change at most
 // vstep_max.  A voxel that passes stores its new state and its ionic
-// dV/dt for the macro step in `rate`; during the next kSurSteps steps
+// dV/dt for the macro step in `rate`; during the next nsub steps
 // k_sur_substep moves its V by that rate plus diffusion only.  Every other
 // voxel gets rate = NaN and joins the list of voxels that k_grid_step
 // advances with the plain step.

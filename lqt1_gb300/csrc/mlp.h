@@ -3,8 +3,9 @@
 // Inputs (48): the 38 evolving states of a cell (V, 8 concentrations, the 29
 // gates/fluxes that change) and 6 parameters (GKs, PCa and GKs-ISO factors of
 // the cell's model, endo/epi/M one-hot), normalised per feature, zero padded.
-// Outputs (48): the normalised change of the 38 states over one macro step of
-// 0.1 ms without diffusion or stimulus, zero padded.
+// Outputs (48): the normalised correction of the 38 states over one macro step
+// (nsub plain steps minus one coarse step) without diffusion or stimulus, zero
+// padded.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>

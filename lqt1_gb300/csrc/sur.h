@@ -11,6 +11,12 @@
 namespace lqt {
 
 constexpr int kSurSteps = 5;     // plain steps per surrogate macro step (0.1 ms at dt = 0.02 ms)
+// A macro-step length (plain steps per macro step) must divide the 50-step
+// span of a captured step graph, so that every graph starts on a macro-step
+// boundary: 1, 2, 5, 10, 25 or 50.  0 in the C ABI selects kSurSteps.
+constexpr int kSurSpan = 50;
+inline bool sur_nsub_ok(int n) { return n >= 1 && n <= kSurSpan && kSurSpan % n == 0; }
+inline int sur_nsub_or_default(int n) { return n == 0 ? kSurSteps : n; }
 constexpr int kSurFeat = 44;     // raw features: 38 states + GKs, PCa, GKs-ISO factors + endo/epi/M one-hot
 
 // One paced cell of the training-data generator.
@@ -45,7 +51,8 @@ uint32_t sur_grid_smem_bytes();
 
 cudaError_t launch_sur_datagen(const SurCell *cells, int64_t ncells, const ModelK *models, const StepK &k,
                                const StepK &kmac, float *X, float *D, unsigned long long *counter, int64_t cap,
-                               uint64_t seed, float dvdt_max, float prob, float jitter, cudaStream_t st);
+                               uint64_t seed, float dvdt_max, float prob, float jitter, int nsub,
+                               cudaStream_t st);
 cudaError_t launch_sur_prepare(const float *X, const float *D, const int64_t *idx, int64_t n, const float *norm,
                                __nv_bfloat16 *xb, float *t, cudaStream_t st);
 

@@ -150,16 +150,18 @@ class Sim:
 
     # ---- learned surrogate ---------------------------------------------------------
     def set_surrogate(self, mlp=None, *, dvdt_max: float = 1.0, kappa: float = 1.5, vstep_max: float = 0.3,
-                      use_net: bool = True):
+                      use_net: bool = True, nsub: int | None = None):
         """Attach a trained surrogate network (lqt1_gb300.surrogate.Mlp) or
-        detach (None).  Mixed form only; see lqt_sim_set_surrogate."""
+        detach (None).  Mixed form only; see lqt_sim_set_surrogate.  The macro
+        step is the network's own length (mlp.nsub plain steps) unless nsub
+        overrides it."""
         L = N.lib()
         L.lqt_sim_set_surrogate.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         if mlp is None:
             N.check(L.lqt_sim_set_surrogate(self._h, None, None), "lqt_sim_set_surrogate")
             self._sur = None
             return
-        cfg = N.SurConfig(dvdt_max, kappa, vstep_max, int(bool(use_net)), 0)
+        cfg = N.SurConfig(dvdt_max, kappa, vstep_max, int(bool(use_net)), int(nsub or getattr(mlp, "nsub", 5)))
         N.check(L.lqt_sim_set_surrogate(self._h, mlp._h, C.byref(cfg)), "lqt_sim_set_surrogate")
         self._sur = mlp     # keep the network alive while attached
 

@@ -48,6 +48,7 @@ class Mlp:
         N.check(self.L.lqt_mlp_create(seed, C.c_void_p(stream or 0), C.byref(h)), "lqt_mlp_create")
         self._h = h
         self.nparam = int(self.L.lqt_mlp_num_params())
+        self.nsub = 5       # plain steps per macro step the network was trained for
 
     def close(self):
         if getattr(self, "_h", None):
@@ -105,7 +106,7 @@ class Mlp:
 class SurRanges(C.Structure):
     _fields_ = [("gks", C.c_double * 2), ("pca", C.c_double * 2), ("iso", C.c_double * 2), ("bcl", C.c_double * 2),
                 ("beats_warm", C.c_int32), ("beats_record", C.c_int32), ("dt", C.c_double), ("dvdt_max", C.c_double),
-                ("prob", C.c_double), ("jitter", C.c_double)]
+                ("prob", C.c_double), ("jitter", C.c_double), ("nsub", C.c_int32), ("reserved", C.c_int32)]
 
 
 def _bind_sur():
@@ -121,16 +122,16 @@ def _bind_sur():
 
 def generate(ncells=65536, seed=1, cap=20_000_000, *, gks=(0.05, 1.0), pca=(1.0, 2.2), iso=(1.0, 2.0),
              bcl=(400.0, 2000.0), beats_warm=0, beats_record=6, dvdt_max=2.0, prob=0.005, jitter=0.3, dt=0.02,
-             stream=None):
+             nsub=5, stream=None):
     """Training pairs from the plain mixed-form integrator on the GPU.
-    Returns torch tensors X [n, 44] (raw features) and D [n, 38] (fine minus
-    coarse state after 0.1 ms)."""
+    Returns torch tensors X [n, 44] (raw features) and D [n, 38] (state after
+    nsub plain steps of dt minus the state after one coarse step of nsub * dt)."""
     import torch
     L = _bind_sur()
     X = torch.empty((cap, 44), dtype=torch.float32, device="cuda")
     D = torch.empty((cap, N_STATE), dtype=torch.float32, device="cuda")
     r = SurRanges((C.c_double * 2)(*gks), (C.c_double * 2)(*pca), (C.c_double * 2)(*iso), (C.c_double * 2)(*bcl),
-                  beats_warm, beats_record, dt, dvdt_max, prob, jitter)
+                  beats_warm, beats_record, dt, dvdt_max, prob, jitter, nsub, 0)
     n = C.c_int64()
     N.check(L.lqt_sur_datagen(ncells, seed, C.byref(r), X.data_ptr(), D.data_ptr(), cap, C.byref(n),
                               C.c_void_p(stream or 0)), "lqt_sur_datagen")
@@ -142,15 +143,15 @@ REF_INDEX = [0] + list(range(1, 9)) + [9 + (j if j < 3 else j + 2) for j in rang
 
 
 def tissue_pairs(n_target=6_000_000, *, sheets=4, n=160, t_end=900.0, grab_every=2.0, dvdt_max=2.0, seed=7,
-                 gks=(0.05, 1.0), pca=(1.0, 2.2), iso=(1.0, 2.0), log=print):
+                 gks=(0.05, 1.0), pca=(1.0, 2.2), iso=(1.0, 2.0), nsub=5, log=print):
     """Training pairs from tissue: 2D sheets in the layout of the 600 x 600
     S1-S2 workload (n x n at 0.15 mm, endo/M/epi bands, S1 line, S2 quadrant at
     a seeded coupling interval U[300, 360] ms), each with a seeded model, run
     with the plain mixed-form integrator.  Every `grab_every` ms the voxels
     with |dV/dt| <= dvdt_max over the last step are sampled; the targets are
     computed on the GPU from those states exactly as k_sur_datagen computes
-    them (5 plain steps of 0.02 ms minus one coarse step of 0.1 ms, no
-    diffusion, no stimulus).  Returns torch tensors X [m, 44], D [m, 38]."""
+    them (nsub plain steps of 0.02 ms minus one coarse step of nsub * 0.02
+    ms, no diffusion, no stimulus).  Returns torch tensors X [m, 44], D [m, 38]."""
     import torch
 
     from . import geometry
@@ -190,10 +191,10 @@ def tissue_pairs(n_target=6_000_000, *, sheets=4, n=160, t_end=900.0, grab_every
         cl = np.concatenate(sel_cls)
         fine = TPORdCells(ty, precision=N.MIXED, model=m, dt=0.02)
         fine.set_state(st)
-        fine.update(kSurStepsPy)
+        fine.update(nsub)
         xf = fine.get_state()
         fine.close()
-        coarse = TPORdCells(ty, precision=N.MIXED, model=m, dt=0.02 * kSurStepsPy)
+        coarse = TPORdCells(ty, precision=N.MIXED, model=m, dt=0.02 * nsub)
         coarse.set_state(st)
         coarse.update(1)
         xc = coarse.get_state()
@@ -206,9 +207,6 @@ def tissue_pairs(n_target=6_000_000, *, sheets=4, n=160, t_end=900.0, grab_every
         D.append(torch.from_numpy((xf - xc)[:, REF_INDEX].astype(np.float32)))
         log(f"tissue sheet {k}: model gks {g_:.2f} pca {p_:.2f} iso {i_:.2f}, S2 at {ci:.1f} ms, {len(st)} pairs")
     return torch.cat(X).cuda(), torch.cat(D).cuda()
-
-
-kSurStepsPy = 5
 
 
 def fit_bounds(D, out_scale):
@@ -315,21 +313,26 @@ def load(path: str | None = None, stream: int | None = None) -> Mlp:
     if "out_bound" in z.files and np.isfinite(z["out_bound"]).all():
         m.set_bounds(z["out_bound"])
     m.meta = json.loads(str(z["meta"]))
+    m.nsub = int(m.meta.get("macro_steps", 5))
     return m
 
 
-def train_default(out=DEFAULT_WEIGHTS, *, ncells=65536, cap=20_000_000, prob=0.005, epochs=12, batch=8192,
-                  lr=2e-3, seed=1, tissue=0, log=print):
+def train_default(out=DEFAULT_WEIGHTS, *, ncells=65536, cap=20_000_000, prob=None, epochs=20, batch=8192,
+                  lr=2e-3, seed=1, tissue=0, nsub=10, log=print):
     """Generate the pairs (paced single cells with the sweep's parameter
     ranges, plus `tissue` pairs from 2D S1-S2 sheets), fit the normalisation,
-    train, validate, save."""
+    train, validate, save.  The defaults reproduce the shipped network: macro
+    steps of 10 plain steps (0.2 ms), recording probability 0.001 * nsub
+    (about cap pairs from 6 beats of 65,536 cells), 20 epochs."""
+    if prob is None:
+        prob = 0.001 * nsub
     import time
 
     import torch
     t0 = time.perf_counter()
-    X, D = generate(ncells=ncells, cap=cap - tissue, prob=prob * (cap - tissue) / cap, seed=seed)
+    X, D = generate(ncells=ncells, cap=cap - tissue, prob=prob * (cap - tissue) / cap, seed=seed, nsub=nsub)
     if tissue > 0:
-        Xt, Dt = tissue_pairs(tissue, seed=seed + 6, log=log)
+        Xt, Dt = tissue_pairs(tissue, seed=seed + 6, nsub=nsub, log=log)
         X, D = torch.cat([X, Xt]), torch.cat([D, Dt])
         del Xt, Dt
         # one shuffle, so that the held-out tail mixes both sources
@@ -341,6 +344,7 @@ def train_default(out=DEFAULT_WEIGHTS, *, ncells=65536, cap=20_000_000, prob=0.0
     t1 = time.perf_counter()
     log(f"pairs {X.shape[0]} ({X.shape[0] - tissue if tissue else X.shape[0]} single-cell) in {t1 - t0:.1f} s")
     m = Mlp(seed=seed)
+    m.nsub = nsub
     im, isc, osc = fit_norm(X, D)
     m.set_norm(im, isc, osc)
     m.set_bounds(fit_bounds(D, osc))
@@ -349,8 +353,8 @@ def train_default(out=DEFAULT_WEIGHTS, *, ncells=65536, cap=20_000_000, prob=0.0
     t2 = time.perf_counter()
     rel = val["rmse"] / np.maximum(val["zero_rmse"], 1e-30)
     meta = dict(pairs=int(X.shape[0]), tissue_pairs=int(tissue), ncells=ncells, epochs=epochs, batch=batch, lr=lr,
-                seed=seed, dt=0.02,
-                macro_steps=5, gen_s=t1 - t0, train_s=t2 - t1, loss_history=[(int(k), float(l)) for k, l in hist],
+                seed=seed, dt=0.02, prob=prob,
+                macro_steps=nsub, gen_s=t1 - t0, train_s=t2 - t1, loss_history=[(int(k), float(l)) for k, l in hist],
                 val_rmse=val["rmse"].tolist(), val_zero_rmse=val["zero_rmse"].tolist(), val_n=int(val["n"]),
                 state_names=STATE_NAMES)
     save(m, out, meta)
@@ -373,15 +377,16 @@ def main():
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
     ap.add_argument("--cells", type=int, default=65536)
     ap.add_argument("--pairs", type=int, default=20_000_000)
-    ap.add_argument("--prob", type=float, default=0.005)
-    ap.add_argument("--epochs", type=int, default=12)
+    ap.add_argument("--prob", type=float, default=None, help="recording probability (default 0.001 * nsub)")
+    ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--batch", type=int, default=8192)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--tissue", type=int, default=0, help="pairs from 2D S1-S2 sheets mixed in (0 = none)")
+    ap.add_argument("--nsub", type=int, default=10, help="plain steps per macro step (divides 50)")
     a = ap.parse_args()
     train_default(a.out, ncells=a.cells, cap=a.pairs, prob=a.prob, epochs=a.epochs, batch=a.batch, lr=a.lr,
-                  seed=a.seed, tissue=a.tissue, log=lambda m: print(m, flush=True))
+                  seed=a.seed, tissue=a.tissue, nsub=a.nsub, log=lambda m: print(m, flush=True))
 
 
 if __name__ == "__main__":
