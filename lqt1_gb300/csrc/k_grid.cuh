@@ -135,22 +135,12 @@ template <typename R> __device__ __forceinline__ void grid_count_bad(const GridD
     if (m && (threadIdx.x & 31) == __ffs(m) - 1) atomicAdd(gd.nbad, (unsigned long long)__popc(m));
 }
 
-// MINB = minimum resident CTAs per SM the register allocation must allow
-// (occupancy variants picked at run time by the autotuner in api_sim.cu; they
-// differ only in register allocation, not in arithmetic).  With the learned
-// surrogate attached, the launch covers only the voxels listed in plist (the
-// ones that run the plain step during the current macro step).
-template <typename R, int DIM, int MINB>
-__global__ void __launch_bounds__(256, MINB) k_grid_step(GridDev<R> gd, StepT<R> kst, int cur)
+// One plain step of tissue voxel k: diffusion, stimulus, the TPORd update,
+// the new V, the detector and the blow-up count.
+template <typename R, int DIM>
+__device__ __forceinline__ void grid_step_voxel(const GridDev<R> &gd, const StepT<R> &kst, int cur, int64_t k,
+                                                const Clock &ck)
 {
-    int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (gd.plist) {
-        if (k >= *gd.plist_n) return;
-        k = gd.plist[k];
-    } else if (k >= gd.ntissue) {
-        return;
-    }
-    const Clock ck = *gd.clk;
     const R *__restrict__ V = gd.vg[cur];
     R *__restrict__ Vn = gd.vg[cur ^ 1];
     const int64_t g = DIM == 1 ? k : (int64_t)gd.gidx[k];
@@ -168,6 +158,55 @@ __global__ void __launch_bounds__(256, MINB) k_grid_step(GridDev<R> gd, StepT<R>
     Vn[g] = c.v;
     if (gd.det) grid_detect(gd, ck, k, (float)vc, (float)c.v, (float)o.dvdt);
     grid_count_bad(gd, c.v);
+}
+
+// The same step as a called function: the list kernel's loop keeps only its
+// own index live across voxels instead of constants hoisted out of the step.
+template <typename R, int DIM>
+__device__ __noinline__ void grid_step_voxel_call(const GridDev<R> &gd, const StepT<R> &kst, int cur, int64_t k,
+                                                  const Clock &ck)
+{
+    grid_step_voxel<R, DIM>(gd, kst, cur, k, ck);
+}
+
+// MINB = minimum resident CTAs per SM the register allocation must allow
+// (occupancy variants picked at run time by the autotuner in api_sim.cu; they
+// differ only in register allocation, not in arithmetic).  One thread per
+// tissue voxel.
+template <typename R, int DIM, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_grid_step(GridDev<R> gd, StepT<R> kst, int cur)
+{
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= gd.ntissue) return;
+    grid_step_voxel<R, DIM>(gd, kst, cur, k, *gd.clk);
+}
+
+// With the learned surrogate attached: the plain step of the voxels listed in
+// plist (plist_n of them, written by the macro-step kernel), grid-stride over
+// a launch of a few waves of CTAs, so that a short list costs its own voxels
+// and not a pass over every tissue voxel.  The step is a called function at 2
+// CTAs/SM (128 registers): inlined into the loop, constants hoisted out of
+// the step stay live across voxels and spill.
+template <typename R, int DIM>
+__global__ void __launch_bounds__(256, 2) k_grid_step_list(GridDev<R> gd, StepT<R> kst, int cur)
+{
+    const int64_t n = *gd.plist_n;
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Clock ck = *gd.clk;
+    for (; i < n; i += (int64_t)gridDim.x * blockDim.x) grid_step_voxel_call<R, DIM>(gd, kst, cur, gd.plist[i], ck);
+}
+
+// CTAs of a list-step launch: four waves at 2 CTAs/SM, never more than one
+// thread per tissue voxel.
+inline unsigned grid_list_blocks(int64_t ntissue)
+{
+    int dev = 0, nsm = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t full = (ntissue + 255) / 256;
+    const int64_t cap = (int64_t)nsm * 2 * 4;
+    return (unsigned)(full < cap ? (full < 1 ? 1 : full) : cap);
 }
 
 // Inside a surrogate macro step: the voxels whose ionic change is fixed

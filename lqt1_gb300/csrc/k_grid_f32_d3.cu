@@ -6,6 +6,10 @@ namespace lqt {
 
 cudaError_t launch_f32_d3(const GridDev<float> &gd, const StepT<float> &kk, int cur, int minb, cudaStream_t st)
 {
+    if (gd.plist) {
+        k_grid_step_list<float, 3><<<grid_list_blocks(gd.ntissue), 256, 0, st>>>(gd, kk, cur);
+        return cudaGetLastError();
+    }
     const unsigned nb = (unsigned)((gd.ntissue + 255) / 256);
     if (minb >= 4) k_grid_step<float, 3, 4><<<nb, 256, 0, st>>>(gd, kk, cur);
     else if (minb == 3) k_grid_step<float, 3, 3><<<nb, 256, 0, st>>>(gd, kk, cur);

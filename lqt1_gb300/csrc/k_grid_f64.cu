@@ -7,6 +7,7 @@ namespace lqt {
 template <> cudaError_t launch_grid_step_minb<double>(const GridDev<double> &gd, const StepT<double> &kk, int cur,
                                                       int dim, int minb, cudaStream_t st)
 {
+    if (gd.plist) return cudaErrorInvalidValue;   // the surrogate's voxel list exists in the mixed form only
     const unsigned nb = (unsigned)((gd.ntissue + 255) / 256);
     if (dim == 1) k_grid_step<double, 1, 1><<<nb, 256, 0, st>>>(gd, kk, cur);
     else if (dim == 2) {
