@@ -285,6 +285,7 @@ def main():
     n = sim.n
     sim.step(args.prerun)
     variant, tune_ms = sim.tune(-1)          # occupancy variant of the plain step kernel
+    sub_variant, sub_ms = sim.substep_variant(-1, timings=True)   # and of the V-only substep
     sim.step(args.warmup)
     sim.surrogate_stats(reset=True)
     with ClockSampler(dev) as clk:
@@ -434,7 +435,10 @@ def main():
                        "l2": "inputs larger than L2 (state %.2f GB)" % (BYTES_MIXED * n / 1e9),
                        "parallelism": f"replicas x{world}",
                        "step_kernel_variant": {"min_ctas_per_sm": variant,
-                                               "tuned_ms": [round(float(x), 4) for x in tune_ms[:3]]}},
+                                               "tuned_ms": [round(float(x), 4) for x in tune_ms[:3]]},
+                       "substep_variant": {"chosen": sub_variant,
+                                           "tuned_ms": dict(zip(("5", "6", "8", "105", "106", "108"),
+                                                                (round(float(x), 4) for x in sub_ms)))}},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "surrogate": surrogate, "mixed_form": mixed,
             "fp64_form": fp64, "accuracy": accuracy, "batched_sweep": sweep, "other_configs": configs,
             "gpu_launches": launches,

@@ -328,6 +328,18 @@ int lqt_sim_get_detect(lqt_sim *s, float *t_act_host, float *apd90_host,
  * ms_per_variant: up to 4 timings (or NULL). */
 int lqt_sim_tune(lqt_sim *s, int32_t variant, int32_t *chosen, float *ms_per_variant);
 
+/* Kernel of the V-only substep inside a surrogate macro step: 5, 6, 8 = one
+ * thread per voxel with direct loads, at that many CTAs/SM; 105, 106, 108 =
+ * persistent CTAs that stage each 256-voxel tile's streamed rows (rate, index,
+ * tensor, control, detector flag) in shared memory with bulk asynchronous
+ * copies, two tiles in flight, at 5, 6, 8 CTAs/SM (2D/3D anisotropic grids;
+ * elsewhere the direct kernel runs).  variant >= 0 forces one (the autotuner
+ * then keeps it); variant < 0 only reports the current one.  All variants give
+ * bit-identical results.  ms_per_variant (or NULL): 6 mean milliseconds per
+ * step from the last autotune, in the order 5, 6, 8, 105, 106, 108 (zeros if
+ * it has not run). */
+int lqt_sim_substep_variant(lqt_sim *s, int32_t variant, int32_t *chosen, float *ms_per_variant);
+
 /* Instrumentation (no counterpart in the reference, which has no timing):
  * run nsteps steps without graph capture, timing each launch of the fused
  * step kernel, of the ghost/clock kernel and (with a surrogate attached) of
@@ -535,10 +547,17 @@ typedef struct lqt_sur_config {
 } lqt_sur_config;
 int lqt_sim_set_surrogate(lqt_sim *s, lqt_mlp *m, const lqt_sur_config *cfg);
 /* Counters since the last reset: macro steps launched, voxel offers, voxels
- * accepted; wait_timeouts = 1 if a tensor-core completion wait ran out (the
- * affected voxels ran the plain step).  reset != 0 zeroes them. */
+ * accepted; wait_timeouts: bit 0 set if a tensor-core completion wait of the
+ * macro step ran out (the affected voxels ran the plain step), bit 1 if a
+ * tile-copy wait of the staged substep ran out (that CTA's remaining voxels
+ * missed the substep: the run is not valid).  reset != 0 zeroes them. */
 int lqt_sim_surrogate_stats(lqt_sim *s, int64_t *macro_steps, int64_t *offered,
                             int64_t *accepted, int32_t *wait_timeouts, int32_t reset);
+/* Offered voxels that failed each residual check since the last reset (a voxel
+ * can fail several): counts[0] a normalised correction beyond kappa times its
+ * bound, [1] a gate outside [0, 1] or not finite, [2] a concentration not
+ * positive, [3] the ionic V change beyond vstep_max. */
+int lqt_sim_surrogate_rejections(lqt_sim *s, int64_t *counts);
 
 /* ======================================================================== *
  *  Synthetic geometries (seeded).  The reference reads its geometry from

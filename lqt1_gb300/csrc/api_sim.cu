@@ -76,7 +76,9 @@ struct lqt_sim {
     int64_t *ecg_count = nullptr, ecg_cap = 0;
     // occupancy variant of k_grid_step (minimum CTAs/SM) and the autotuner
     int minb = 2;
-    int sub_minb = 5;               // k_sur_substep occupancy variant
+    int sub_minb = 5;               // V-only substep variant (kSubVariants)
+    bool sub_forced = false;        // set by lqt_sim_substep_variant: the autotuner keeps it
+    float sub_tune_ms[kSubNVariants] = {};   // last autotune: mean ms per substep variant
     bool tuned = false;
     float tune_ms[4] = {0, 0, 0, 0};
     // learned surrogate (mixed form): network, per-voxel rate, counters
@@ -166,6 +168,7 @@ struct lqt_sim {
         g.sdflag = in_macro ? sdflag : nullptr;
         g.plist = in_macro ? plist : nullptr;
         g.plist_n = in_macro ? (const int64_t *)plist_n : nullptr;
+        g.serr = in_macro ? sur_err : nullptr;
         return g;
     }
     double diso = 0.154;
@@ -374,10 +377,10 @@ int autotune(lqt_sim *s, int per, int64_t *consumed)
     s->minb = best_m;
     // with a surrogate attached: the V-only substep's variant, timed the same
     // way (variants in turn, whole steps, the first round discarded)
-    if (rc == LQT_OK && s->sur && !s->fp64()) {
-        float ts[3] = {0, 0, 0};
+    if (rc == LQT_OK && s->sur && !s->fp64() && !s->sub_forced) {
+        float ts[kSubNVariants] = {};
         for (int i = 0; i < per && rc == LQT_OK; ++i) {
-            for (int c = 0; c < 3 && rc == LQT_OK; ++c) {
+            for (int c = 0; c < kSubNVariants && rc == LQT_OK; ++c) {
                 s->sub_minb = kSubVariants[c];
                 rc = launch_sur_if_due(s);
                 if (rc) break;
@@ -403,8 +406,9 @@ int autotune(lqt_sim *s, int per, int64_t *consumed)
             }
         }
         int bs = 0;
-        for (int c = 1; c < 3; ++c)
+        for (int c = 1; c < kSubNVariants; ++c)
             if (ts[c] < ts[bs]) bs = c;
+        for (int c = 0; c < kSubNVariants; ++c) s->sub_tune_ms[c] = per > 1 ? ts[c] / (per - 1) : ts[c];
         s->sub_minb = kSubVariants[bs];
     }
     cudaEventDestroy(a);
@@ -575,17 +579,18 @@ int lqt_sim_create(const lqt_sim_params *params, const lqt_geometry *geom, lqt_s
     rc |= s->mem.alloc(&s->vg[1], s->ngrid * rsz);
     rc |= s->mem.alloc(&s->gate, s->ld * rsz * kNGate);
     rc |= s->mem.alloc((void **)&s->conc, s->ld * 8 * kNConc);
-    rc |= s->mem.alloc((void **)&s->ctl, n);
+    const int64_t npad = pad_tiles(n);     // per-voxel rows the staged substep copies in whole tiles
+    rc |= s->mem.alloc((void **)&s->ctl, npad);
     rc |= s->mem.alloc((void **)&s->clk, sizeof(Clock));
     rc |= s->mem.alloc((void **)&s->nbad, sizeof(unsigned long long));
     if (dim > 1) {
-        rc |= s->mem.alloc((void **)&s->gidx, n * 4);
+        rc |= s->mem.alloc((void **)&s->gidx, npad * 4);
         rc |= s->mem.alloc((void **)&s->bnd_dst, std::max<int64_t>(1, s->nbnd) * 4);
         rc |= s->mem.alloc((void **)&s->bnd_src, std::max<int64_t>(1, s->nbnd) * 4);
     }
     if (dim > 1 && geom->fibre) {
-        rc |= s->mem.alloc(&s->d6, n * 6 * rsz);
-        rc |= s->mem.alloc(&s->b3, n * 3 * rsz);
+        rc |= s->mem.alloc(&s->d6, npad * 6 * rsz);
+        rc |= s->mem.alloc(&s->b3, npad * 3 * rsz);
     }
     if (dim == 1) {
         rc |= s->mem.alloc(&s->coeff, n * rsz);
@@ -620,7 +625,12 @@ int lqt_sim_create(const lqt_sim_params *params, const lqt_geometry *geom, lqt_s
         bd[j] = (int32_t)s->tm.bnd_dst[j];
         bs[j] = (int32_t)s->tm.bnd_src[j];
     }
-    cudaError_t e = cudaMemcpyAsync(s->ctl, s->ctl_host.data(), n, cudaMemcpyHostToDevice, st);
+    // tile padding past the last voxel: zero (copied, never stepped)
+    cudaError_t e = cudaMemsetAsync(s->ctl, 0, npad, st);
+    if (e == cudaSuccess && dim > 1) e = cudaMemsetAsync(s->gidx, 0, npad * 4, st);
+    if (e == cudaSuccess && s->d6) e = cudaMemsetAsync(s->d6, 0, npad * 6 * rsz, st);
+    if (e == cudaSuccess && s->b3) e = cudaMemsetAsync(s->b3, 0, npad * 3 * rsz, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->ctl, s->ctl_host.data(), n, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && dim > 1) e = cudaMemcpyAsync(s->gidx, gi32.data(), n * 4, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && s->nbnd) e = cudaMemcpyAsync(s->bnd_dst, bd.data(), s->nbnd * 4, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && s->nbnd) e = cudaMemcpyAsync(s->bnd_src, bs.data(), s->nbnd * 4, cudaMemcpyHostToDevice, st);
@@ -996,6 +1006,22 @@ int lqt_sim_tune(lqt_sim *s, int32_t variant, int32_t *chosen, float *ms_per_var
     return LQT_OK;
 }
 
+int lqt_sim_substep_variant(lqt_sim *s, int32_t variant, int32_t *chosen, float *ms_per_variant)
+{
+    if (!s) return fail(LQT_ERR_INVALID, "lqt_sim_substep_variant: NULL handle");
+    if (variant >= 0) {
+        bool ok = false;
+        for (int c = 0; c < kSubNVariants; ++c) ok |= kSubVariants[c] == variant;
+        if (!ok) return fail(LQT_ERR_INVALID, "lqt_sim_substep_variant: variant must be 5, 6, 8, 105, 106 or 108");
+        s->sub_minb = variant;
+        s->sub_forced = true;
+        s->graph_valid = false;
+    }
+    if (chosen) *chosen = s->sub_minb;
+    if (ms_per_variant) std::memcpy(ms_per_variant, s->sub_tune_ms, sizeof(s->sub_tune_ms));
+    return LQT_OK;
+}
+
 int lqt_sim_profile(lqt_sim *s, int64_t nsteps, double *ms_step, double *ms_ghost, double *ms_sur)
 {
     if (!s || nsteps <= 0) return fail(LQT_ERR_INVALID, "lqt_sim_profile: NULL handle or nsteps <= 0");
@@ -1105,24 +1131,38 @@ int lqt_sim_set_surrogate(lqt_sim *s, lqt_mlp *m, const lqt_sur_config *cfg)
     const float *nrm = nullptr;
     if (!mlp_device_view(m, &w, &nrm)) return fail(LQT_ERR_INVALID, "lqt_sim_set_surrogate: network not initialised");
     if (!s->srate) {
-        int rc = s->mem.alloc((void **)&s->srate, s->ntissue * 4) |
+        int rc = s->mem.alloc((void **)&s->srate, pad_tiles(s->ntissue) * 4) |
                  s->mem.alloc((void **)&s->plist, s->ntissue * 4) |
-                 s->mem.alloc((void **)&s->sdflag, s->ntissue) |
+                 s->mem.alloc((void **)&s->sdflag, pad_tiles(s->ntissue)) |
                  s->mem.alloc((void **)&s->plist_n, sizeof(unsigned long long)) |
-                 s->mem.alloc((void **)&s->sur_stats, 2 * sizeof(unsigned long long)) |
+                 s->mem.alloc((void **)&s->sur_stats, kSurNStats * sizeof(unsigned long long)) |
                  s->mem.alloc((void **)&s->sur_err, sizeof(int));
         if (rc) return LQT_ERR_NOMEM;
-        CK(cudaMemsetAsync(s->sur_stats, 0, 2 * sizeof(unsigned long long), s->stream));
+        CK(cudaMemsetAsync(s->sur_stats, 0, kSurNStats * sizeof(unsigned long long), s->stream));
+        CK(cudaMemsetAsync(s->sdflag, 0, pad_tiles(s->ntissue), s->stream));
         CK(cudaMemsetAsync(s->sur_err, 0, sizeof(int), s->stream));
     }
-    // NaN everywhere: plain steps until the first macro-step boundary
-    CK(cudaMemsetAsync(s->srate, 0xff, s->ntissue * 4, s->stream));
+    // NaN everywhere (the tile padding included): plain steps until the first
+    // macro-step boundary
+    CK(cudaMemsetAsync(s->srate, 0xff, pad_tiles(s->ntissue) * 4, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     s->sur = m;
     s->sur_cfg = *cfg;
     s->sur_nsub = sur_nsub_or_default(cfg->nsub);
     s->plist_valid = false;
     s->graph_valid = false;
+    return LQT_OK;
+}
+
+int lqt_sim_surrogate_rejections(lqt_sim *s, int64_t *counts)
+{
+    if (!s || !counts) return fail(LQT_ERR_INVALID, "lqt_sim_surrogate_rejections: NULL argument");
+    unsigned long long st[kSurNStats] = {};
+    if (s->sur_stats) {
+        CK(cudaStreamSynchronize(s->stream));
+        CK(cudaMemcpy(st, s->sur_stats, sizeof(st), cudaMemcpyDeviceToHost));
+    }
+    for (int r = 0; r < 4; ++r) counts[r] = (int64_t)st[2 + r];
     return LQT_OK;
 }
 
@@ -1142,7 +1182,7 @@ int lqt_sim_surrogate_stats(lqt_sim *s, int64_t *macro_steps, int64_t *offered, 
     if (accepted) *accepted = (int64_t)st[1];
     if (wait_timeouts) *wait_timeouts = err;
     if (reset && s->sur_stats) {
-        CK(cudaMemset(s->sur_stats, 0, sizeof(st)));
+        CK(cudaMemset(s->sur_stats, 0, kSurNStats * sizeof(unsigned long long)));
         CK(cudaMemset(s->sur_err, 0, sizeof(int)));
         s->sur_launches = 0;
     }

@@ -59,7 +59,14 @@ template <typename R> struct GridDev {
     const uint8_t *sdflag;         // 1 = the voxel's detector runs during the macro step
     const int32_t *plist;
     const int64_t *plist_n;
+    int *serr;                     // bit 1 set when a substep's copy wait ran out
 };
+
+// Voxels per tile of the staged substep kernel; the per-voxel arrays it
+// streams (control bytes, dense index, tensor, divergence, rate, detector
+// flag) are allocated in whole tiles, so every tile copy is in bounds.
+constexpr int kSubTile = 256;
+inline int64_t pad_tiles(int64_t n) { return (n + kSubTile - 1) / kSubTile * kSubTile; }
 
 // Occupancy variants of k_grid_step: minimum CTAs/SM of 256 threads.
 constexpr int kGridVariantsF32[3] = {2, 3, 4};
@@ -70,8 +77,13 @@ cudaError_t launch_grid_step(const GridDev<R> &gd, const StepK &k, int cur, int 
 template <typename R>
 cudaError_t launch_grid_step_minb(const GridDev<R> &gd, const StepT<R> &k, int cur, int dim, int minb, cudaStream_t st);
 template <typename R> cudaError_t launch_ghost(const GridDev<R> &gd, int nxt, cudaStream_t st);
-// Occupancy variants of k_sur_substep: minimum CTAs/SM of 256 threads.
-constexpr int kSubVariants[3] = {5, 6, 8};
+// Variants of the V-only substep: minimum CTAs/SM of 256 threads of
+// k_sur_substep (5, 6, 8: one thread per voxel, direct loads) or of
+// k_sur_substep_tile (100 + CTAs/SM: persistent CTAs, each tile's streamed
+// rows staged in shared memory by bulk asynchronous copies; 2D/3D
+// anisotropic grids, the others fall back to the direct kernel).
+constexpr int kSubVariants[6] = {5, 6, 8, 105, 106, 108};
+constexpr int kSubNVariants = 6;
 cudaError_t launch_sur_substep(const GridDev<float> &gd, double dt, int cur, int dim, int minb, cudaStream_t st);
 template <typename R>
 cudaError_t launch_ecg(const GridDev<R> &gd, int cur, const float4 *el, int nel, double *partial, double *out,

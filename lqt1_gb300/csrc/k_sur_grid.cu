@@ -3,10 +3,11 @@
 // At every macro-step boundary (every nsub plain steps) one persistent
 // kernel walks the tissue voxels in tiles of 128.  A voxel is offered to the
 // surrogate when |dV/dt| over the last plain step (both V buffers are still
-// resident) is at most dvdt_max, no stimulus reaches it during the macro step
-// and its AP detector is not inside an upstroke (activation seen, peak not yet
-// found: the overshoot that sets the APD90 level is always taken by plain
-// steps).  For the offered voxels of a tile
+// resident) is at most dvdt_max and no stimulus reaches it during the macro
+// step (the fast upstroke always takes plain steps; a slow rise into the dome
+// may take macro steps, with the detector run at every substep so that the
+// running peak that sets the APD90 level is kept).  For the offered voxels of
+// a tile
 //   1. each thread writes its voxel's normalised BF16 features into shared
 //      memory (row = thread, tcgen05 K-major core-matrix layout);
 //   2. one elected thread runs the 48 -> 128 -> 128 -> 48 network with
@@ -305,19 +306,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
             const float dv = (vc - Vp[g]) * inv_dt;
             const uint8_t ctl = gd.ctl[k];
             ct = ctl & kCtlType;
-            bool rising = false;
             if (gd.det) {
                 const float4 d = gd.det[k];
                 const uint32_t ph = __float_as_uint(d.w) & 7u;
-                rising = ph == kDetRise;
                 // does the detector need this voxel's substeps?  A cycle that
-                // opens; an activation crossing within reach; in the fall, the
-                // running peak, the 50% (EAD) and the 90% levels
+                // opens; an activation crossing within reach; a slow rise
+                // towards the peak (a dome without a notch: the fast upstroke
+                // is excluded by the dV/dt bound); in the fall, the running
+                // peak, the 50% (EAD) and the 90% levels
                 const float amp = d.y - d.x;
-                need_det = opens || (ph == kDetWait && vc > gd.act_thr - kDetMargin) ||
+                need_det = opens || ph == kDetRise || (ph == kDetWait && vc > gd.act_thr - kDetMargin) ||
                            (ph == kDetFall && !(vc < d.y - kDetMargin && vc > d.y - 0.5f * amp + kDetMargin));
             }
-            elig = net_ok && !rising && fabsf(dv) <= sg.dvdt_max && !stim_ahead(gd, ck, ctl, k, sg.nsub);
+            elig = net_ok && fabsf(dv) <= sg.dvdt_max && !stim_ahead(gd, ck, ctl, k, sg.nsub);
         }
         // 1. features (the previous tile's MMAs have all completed)
         if (use_net) {
@@ -418,6 +419,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
             tpord_step<float>(c, ct, gd.model, sg.kmac, 0.f, 0.f, &o);
         }
         bool ok = elig && (net_ok || !use_net);
+        uint32_t why = 0;   // failed checks: 1 network bound, 2 gate range, 4 concentration, 8 ionic V step
         if (have_net) {
             float2 *cp[8];
             float *gp[29];
@@ -435,7 +437,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
                         const int j = cc + i;
                         if (j < kMlpNState) {
                             const float z = v[i];
-                            ok &= fabsf(z) <= sg.kappa * obd[j];
+                            if (!(fabsf(z) <= sg.kappa * obd[j])) why |= 1u;
                             const float d = z * osc[j];
                             if (j == 0) c.v += d;
                             else if (j < 9) cadd(*cp[j - 1], d);
@@ -453,15 +455,18 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
 #pragma unroll
             for (int j = 0; j < kSurNProb; ++j) {
                 const float x = *gp[j];
-                ok &= x >= -1e-3f && x <= 1.001f;
+                if (!(x >= -1e-3f && x <= 1.001f)) why |= 2u;
                 *gp[j] = fminf(fmaxf(x, 0.f), 1.f);
             }
 #pragma unroll
-            for (int j = kSurNProb; j < 29; ++j) ok &= *gp[j] == *gp[j];
+            for (int j = kSurNProb; j < 29; ++j)
+                if (!(*gp[j] == *gp[j])) why |= 2u;
 #pragma unroll
-            for (int j = 0; j < 8; ++j) ok &= cp[j]->x > 0.f;
+            for (int j = 0; j < 8; ++j)
+                if (!(cp[j]->x > 0.f)) why |= 4u;
             const float dvm = c.v - vc;
-            ok &= fabsf(dvm) <= sg.vstep_max;     // false for NaN as well
+            if (!(fabsf(dvm) <= sg.vstep_max)) why |= 8u;    // NaN fails as well
+            ok = ok && why == 0;
             if (ok) {
                 store_cell(c, gd.s, k);
                 sg.rate[k] = dvm * inv_mac;
@@ -477,6 +482,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
             if (lane == 0) base = atomicAdd(sg.plist_n, (unsigned long long)__popc(mp));
             base = __shfl_sync(0xffffffffu, base, 0);
             if (plain) sg.plist[base + __popc(mp & ((1u << lane) - 1u))] = (int32_t)k;
+        }
+        // offered voxels that failed each check (one atomic per warp and reason)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const unsigned mr = __ballot_sync(0xffffffffu, elig && ((why >> r) & 1u));
+            if (lane == 0 && mr) atomicAdd(sg.stats + 2 + r, (unsigned long long)__popc(mr));
         }
         const unsigned mo = __ballot_sync(0xffffffffu, elig), ma = __ballot_sync(0xffffffffu, ok);
         if (lane == 0) {

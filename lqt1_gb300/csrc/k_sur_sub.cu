@@ -1,20 +1,177 @@
-// k_sur_sub.cu -- the V-only step of the voxels inside a surrogate macro step
-// (k_sur_substep in k_grid.cuh), mixed form, 1D/2D/3D.
+// k_sur_sub.cu -- the V-only step of the voxels inside a surrogate macro step,
+// mixed form, 1D/2D/3D: k_sur_substep (k_grid.cuh, one thread per voxel,
+// direct loads) and k_sur_substep_tile (below, persistent CTAs that stage
+// each tile's streamed rows in shared memory with bulk asynchronous copies).
+#include <atomic>
+#include <cstddef>
+
 #include "k_grid.cuh"
+#include "tc.cuh"
 
 namespace lqt {
 
-template <int MINB> static void launch_minb(const GridDev<float> &gd, double dt, int cur, int dim, unsigned nb,
-                                            cudaStream_t st)
+namespace {
+
+constexpr uint32_t kSubWaitLimit = 1u << 22;   // bounded mbarrier polls per tile
+
+// One tile's rows, in the order of the copies: the macro step's ionic rate,
+// the dense index, the tensor (6 per voxel), its divergence (3 per voxel), the
+// control byte and the detector flag.
+struct __align__(16) SubStage {
+    float rate[kSubTile];
+    int32_t gidx[kSubTile];
+    float d6[kSubTile * 6];
+    float b3[kSubTile * 3];
+    uint8_t ctl[kSubTile];
+    uint8_t flag[kSubTile];
+};
+static_assert(sizeof(SubStage) % 16 == 0 && offsetof(SubStage, gidx) % 16 == 0 && offsetof(SubStage, d6) % 16 == 0 &&
+                  offsetof(SubStage, b3) % 16 == 0 && offsetof(SubStage, ctl) % 16 == 0 &&
+                  offsetof(SubStage, flag) % 16 == 0,
+              "bulk copies need 16-byte aligned destinations");
+
+// Thread 0: the copies of tile k0 / kSubTile into one stage, completing on bar.
+// Every array holds whole tiles (pad_tiles), so each copy is in bounds, and
+// k0 is a multiple of kSubTile, so every source is 16-byte aligned.
+__device__ __forceinline__ void sub_issue(SubStage &sg, uint64_t *bar, const GridDev<float> &gd, int64_t k0, bool det)
+{
+    constexpr uint32_t n = kSubTile;
+    tc::mbar_expect_tx(bar, n * (4 + 4 + 24 + 12 + 1) + (det ? n : 0));
+    tc::bulk_g2s(sg.rate, gd.srate + k0, n * 4, bar);
+    tc::bulk_g2s(sg.gidx, gd.gidx + k0, n * 4, bar);
+    tc::bulk_g2s(sg.d6, gd.d6 + 6 * k0, n * 24, bar);
+    tc::bulk_g2s(sg.b3, gd.b3 + 3 * k0, n * 12, bar);
+    tc::bulk_g2s(sg.ctl, gd.ctl + k0, n, bar);
+    if (det) tc::bulk_g2s(sg.flag, gd.sdflag + k0, n, bar);
+}
+
+}  // namespace
+
+// Persistent: CTA b takes tiles b, b + gridDim.x, ...  Two stages: while the
+// threads step the voxels of one tile (V stencil from the dense grid, through
+// L1/L2), the copy engine brings the next tile's rows, so the streamed bytes
+// stay in flight without a per-thread load chain in front of the stencil.
+// Arithmetic identical to k_sur_substep.  A copy wait that runs out sets bit 1
+// of *serr; the CTA waits (bounded) for its copies still in flight and leaves
+// its remaining tiles unstepped.
+template <int DIM, int MINB>
+__global__ void __launch_bounds__(kSubTile, MINB) k_sur_substep_tile(GridDev<float> gd, float dt, int cur)
+{
+    __shared__ SubStage stg[2];
+    __shared__ __align__(8) uint64_t bar[2];
+    const int t = threadIdx.x;
+    const int64_t ntiles = (gd.ntissue + kSubTile - 1) / kSubTile;
+    const int64_t stride = gridDim.x;
+    int64_t tile = blockIdx.x;
+    if (tile >= ntiles) return;
+    const bool det = gd.det != nullptr;
+    if (t == 0) {
+        tc::mbar_init(&bar[0], 1);
+        tc::mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        sub_issue(stg[0], &bar[0], gd, tile * kSubTile, det);
+        if (tile + stride < ntiles) sub_issue(stg[1], &bar[1], gd, (tile + stride) * kSubTile, det);
+    }
+    __syncthreads();
+    const Clock ck = *gd.clk;
+    const float *__restrict__ V = gd.vg[cur];
+    float *__restrict__ Vn = gd.vg[cur ^ 1];
+    for (uint32_t it = 0; tile < ntiles; tile += stride, ++it) {
+        const int s = it & 1;
+        const bool ok = tc::mbar_wait(&bar[s], (it >> 1) & 1, kSubWaitLimit);
+        if (!__syncthreads_and(ok ? 1 : 0)) {
+            if (t == 0) {
+                atomicOr(gd.serr, 2);
+                tc::mbar_wait(&bar[s], (it >> 1) & 1, kSubWaitLimit);
+                if (tile + stride < ntiles) tc::mbar_wait(&bar[s ^ 1], ((it + 1) >> 1) & 1, kSubWaitLimit);
+            }
+            return;
+        }
+        const SubStage &sg = stg[s];
+        const int64_t k = tile * kSubTile + t;
+        const float r = sg.rate[t];
+        if (k < gd.ntissue && r == r) {
+            const int64_t g = sg.gidx[t];
+            float Dt[6], Bt[3];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) Dt[i] = sg.d6[6 * t + i];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) Bt[i] = sg.b3[3 * t + i];
+            const float vc = V[g];
+            const float du = sub_du<DIM>(gd, V, g, k, vc, Dt, Bt);
+            const float ist = grid_stim(gd, ck, sg.ctl[t], k);
+            const float dvdt = r - ist;
+            const float vn = vc + (dvdt + du) * dt;
+            Vn[g] = vn;
+            if (det && sg.flag[t]) grid_detect(gd, ck, k, vc, vn, dvdt);
+            const bool bad = !(vn == vn) || vn < gd.vmin_ok || vn > gd.vmax_ok;
+            if (bad) atomicAdd(gd.nbad, 1ull);
+        }
+        __syncthreads();   // every thread is done with stage s
+        if (t == 0 && tile + 2 * stride < ntiles) {
+            tc::fence_proxy_async();
+            sub_issue(stg[s], &bar[s], gd, (tile + 2 * stride) * kSubTile, det);
+        }
+    }
+}
+
+namespace {
+
+template <int MINB> void launch_minb(const GridDev<float> &gd, double dt, int cur, int dim, unsigned nb, cudaStream_t st)
 {
     if (dim == 1) k_sur_substep<1, MINB><<<nb, 256, 0, st>>>(gd, (float)dt, cur);
     else if (dim == 2) k_sur_substep<2, MINB><<<nb, 256, 0, st>>>(gd, (float)dt, cur);
     else k_sur_substep<3, MINB><<<nb, 256, 0, st>>>(gd, (float)dt, cur);
 }
 
-cudaError_t launch_sur_substep(const GridDev<float> &gd, double dt, int cur, int dim, int minb, cudaStream_t st)
+// The kernel's shared-memory carve-out at its maximum, once per device, so
+// that MINB CTAs of two stages each fit on an SM.
+template <typename K> cudaError_t carveout_once(K kernel, std::atomic<uint64_t> &done)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const uint64_t bit = dev < 64 ? (1ull << dev) : 0;
+    if (bit && (done.load() & bit)) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e == cudaSuccess && bit) done.fetch_or(bit);
+    return e;
+}
+
+template <int DIM, int MINB> cudaError_t launch_tile(const GridDev<float> &gd, double dt, int cur, cudaStream_t st)
+{
+    static std::atomic<uint64_t> done{0};
+    cudaError_t e = carveout_once(k_sur_substep_tile<DIM, MINB>, done);
+    if (e != cudaSuccess) return e;
+    int dev = 0, nsm = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t ntiles = (gd.ntissue + kSubTile - 1) / kSubTile;
+    const int64_t grid = ntiles < (int64_t)nsm * MINB ? ntiles : (int64_t)nsm * MINB;
+    k_sur_substep_tile<DIM, MINB><<<(unsigned)grid, kSubTile, 0, st>>>(gd, (float)dt, cur);
+    return cudaGetLastError();
+}
+
+bool al16(const void *p) { return p && ((uintptr_t)p & 15u) == 0; }
+
+}  // namespace
+
+cudaError_t launch_sur_substep(const GridDev<float> &gd, double dt, int cur, int dim, int variant, cudaStream_t st)
 {
     if (gd.ntissue <= 0) return cudaSuccess;
+    const bool tile = variant >= 100;
+    const int minb = tile ? variant - 100 : variant;
+    if (tile && dim >= 2 && al16(gd.d6) && al16(gd.b3) && al16(gd.srate) && al16(gd.gidx) && al16(gd.ctl) &&
+        gd.serr && (!gd.det || al16(gd.sdflag))) {
+        if (dim == 2) {
+            if (minb == 8) return launch_tile<2, 8>(gd, dt, cur, st);
+            if (minb == 6) return launch_tile<2, 6>(gd, dt, cur, st);
+            return launch_tile<2, 5>(gd, dt, cur, st);
+        }
+        if (minb == 8) return launch_tile<3, 8>(gd, dt, cur, st);
+        if (minb == 6) return launch_tile<3, 6>(gd, dt, cur, st);
+        return launch_tile<3, 5>(gd, dt, cur, st);
+    }
     const unsigned nb = (unsigned)((gd.ntissue + 256 * kSubU - 1) / (256 * kSubU));
     if (minb == 8) launch_minb<8>(gd, dt, cur, dim, nb, st);
     else if (minb == 6) launch_minb<6>(gd, dt, cur, dim, nb, st);

@@ -15,6 +15,10 @@ constexpr int kSurSteps = 5;     // plain steps per surrogate macro step (0.1 ms
 // span of a captured step graph, so that every graph starts on a macro-step
 // boundary: 1, 2, 5, 10, 25 or 50.  0 in the C ABI selects kSurSteps.
 constexpr int kSurSpan = 50;
+// Counters of a tissue run with a surrogate: offered, accepted, and the
+// offered voxels failing each residual check (network bound, gate range,
+// concentration sign, ionic V step).
+constexpr int kSurNStats = 6;
 inline bool sur_nsub_ok(int n) { return n >= 1 && n <= kSurSpan && kSurSpan % n == 0; }
 inline int sur_nsub_or_default(int n) { return n == 0 ? kSurSteps : n; }
 constexpr int kSurFeat = 44;     // raw features: 38 states + GKs, PCa, GKs-ISO factors + endo/epi/M one-hot
@@ -36,7 +40,7 @@ struct SurGrid {
     uint8_t *dflag;                 // per tissue voxel: 1 = its AP detector runs on the substeps
     int32_t *plist;                 // voxels that run the plain step during the macro step
     unsigned long long *plist_n;    // their count (zero before the launch)
-    unsigned long long *stats;      // [0] voxels offered, [1] accepted
+    unsigned long long *stats;      // [0] voxels offered, [1] accepted, [2..5] offered voxels failing a check (kSurNStats)
     int *err;                       // set when an mbarrier wait ran out
     StepT<float> kmac;              // the coarse step (dt = nsub * plain dt)
     float par[3];                   // GKs, PCa and GKs-ISO factors of the model

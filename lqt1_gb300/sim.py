@@ -123,6 +123,17 @@ class Sim:
         N.check(L.lqt_sim_tune(self._h, int(variant), C.byref(ch), _p(ms)), "lqt_sim_tune")
         return ch.value, ms
 
+    def substep_variant(self, variant: int = -1, timings: bool = False):
+        """Force the V-only substep's kernel variant (5, 6, 8 direct; 105, 106,
+        108 staged by bulk copies) or, with -1, report the current one; with
+        timings, also the last autotune's ms per variant (same order)."""
+        L = N.lib()
+        L.lqt_sim_substep_variant.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.c_void_p]
+        ch = C.c_int32()
+        ms = np.zeros(6, np.float32)
+        N.check(L.lqt_sim_substep_variant(self._h, int(variant), C.byref(ch), _p(ms)), "lqt_sim_substep_variant")
+        return (ch.value, ms) if timings else ch.value
+
     def profile(self, nsteps: int = 20):
         """Mean device ms per launch of the fused step kernel, of the ghost
         kernel and (with a surrogate attached) of the surrogate macro-step
@@ -175,6 +186,15 @@ class Sim:
         N.check(L.lqt_sim_surrogate_stats(self._h, C.byref(m), C.byref(o), C.byref(a), C.byref(t), int(reset)),
                 "lqt_sim_surrogate_stats")
         return dict(macro_steps=m.value, offered=o.value, accepted=a.value, wait_timeouts=t.value)
+
+    def surrogate_rejections(self):
+        """Offered voxels that failed each residual check since the last
+        reset: network bound, gate range, concentration, ionic V step."""
+        L = N.lib()
+        L.lqt_sim_surrogate_rejections.argtypes = [C.c_void_p, C.c_void_p]
+        c = np.zeros(4, np.int64)
+        N.check(L.lqt_sim_surrogate_rejections(self._h, _p(c)), "lqt_sim_surrogate_rejections")
+        return dict(zip(("network_bound", "gate_range", "concentration", "v_step"), (int(x) for x in c)))
 
     def boundary(self):
         L = N.lib()

@@ -203,3 +203,42 @@ def test_speed_gain_over_plain_step(lq, torch, net):
         sim.step(10000)
         rates[mode] = sim.n * 10000 / (time.perf_counter() - t0)
     assert rates["net"] > 1.3 * rates["plain"], rates
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_substep_variants_bit_identical(lq, net, dim):
+    """Every kernel of the V-only substep (direct loads at 5 and 8 CTAs/SM;
+    tiles staged in shared memory by bulk copies at 5, 6 and 8 CTAs/SM) gives
+    the same bits: state, V, detector and surrogate counters after the
+    upstroke and into the plateau of an anisotropic grid whose voxel count is
+    not a multiple of the 256-voxel tile."""
+    if dim == 2:
+        sh = lq.geometry.sheet(130, 97, s1_cols=3)
+        nx, ny = sh.types.shape
+        ang = np.linspace(0.0, np.pi / 2, nx)[:, None] * np.ones((1, ny))
+        fibre = np.stack([np.cos(ang), np.sin(ang), np.zeros_like(ang)], -1).astype(np.float32)
+        types, mask, dx = sh.types, sh.s1_mask, 0.15
+    else:
+        v = lq.geometry.ventricle(nx=44, ny=44, nz=50, dx=0.2, a_out=4.0, c_out=8.0, wall=2.0, z_base=9.0,
+                                  island_radius=1.5, stim_radius=1.2)
+        types, fibre, mask, dx = v.types, v.fibre, v.s1_mask, 0.2
+    m = lq.model("baseline", gks_scale=0.5, pca_scale=1.5, gks_iso_scale=1.2)
+    out = {}
+    for var in (5, 8, 105, 106, 108):
+        sim = lq.Sim(types, dx, fibre=fibre, precision=lq.MIXED, model=m)
+        assert sim.n % 256 != 0
+        sim.set_protocol(bcl=1000.0, s1_mask=mask, s1_start=0.0, s1_duration=2.0, s1_strength=-52.0)
+        sim.set_surrogate(net)
+        assert sim.substep_variant(var) == var
+        sim.step(4000)
+        assert sim.substep_variant() == var
+        out[var] = (sim.get_state(), sim.get_v(), sim.detect(), sim.surrogate_stats(), sim.check())
+        sim.close()
+    st0, v0, d0, s0, b0 = out[5]
+    assert b0 == 0 and s0["wait_timeouts"] == 0 and s0["accepted"] > 0.5 * s0["offered"] > 0
+    for var, (st, vv, d, s, b) in out.items():
+        np.testing.assert_array_equal(st, st0, err_msg=f"variant {var}")
+        np.testing.assert_array_equal(vv, v0, err_msg=f"variant {var}")
+        for key in d0:
+            np.testing.assert_array_equal(d[key], d0[key], err_msg=f"variant {var}: {key}")
+        assert s == s0 and b == b0, var
