@@ -46,6 +46,7 @@ struct lqt_sim {
     // device
     void *vg[2] = {nullptr, nullptr};
     void *gate = nullptr, *d6 = nullptr, *b3 = nullptr, *coeff = nullptr, *dcoeff = nullptr;
+    __half2 *d6h = nullptr, *b3h = nullptr;   // FP16 tensor copies for the surrogate substep (pad_tiles rows)
     double *conc = nullptr, *aos = nullptr;
     int32_t *gidx = nullptr, *bnd_dst = nullptr, *bnd_src = nullptr;
     uint8_t *ctl = nullptr;
@@ -169,6 +170,8 @@ struct lqt_sim {
         g.plist = in_macro ? plist : nullptr;
         g.plist_n = in_macro ? (const int64_t *)plist_n : nullptr;
         g.serr = in_macro ? sur_err : nullptr;
+        g.d6h = in_macro ? d6h : nullptr;
+        g.b3h = in_macro ? b3h : nullptr;
         return g;
     }
     double diso = 0.154;
@@ -1141,6 +1144,14 @@ int lqt_sim_set_surrogate(lqt_sim *s, lqt_mlp *m, const lqt_sur_config *cfg)
         CK(cudaMemsetAsync(s->sur_stats, 0, kSurNStats * sizeof(unsigned long long), s->stream));
         CK(cudaMemsetAsync(s->sdflag, 0, pad_tiles(s->ntissue), s->stream));
         CK(cudaMemsetAsync(s->sur_err, 0, sizeof(int), s->stream));
+    }
+    // the substep streams the tensor in FP16 (made once, padded to whole tiles)
+    if (s->d6 && !s->d6h) {
+        const int64_t np = pad_tiles(s->ntissue);
+        if (s->mem.alloc((void **)&s->d6h, np * 12) | s->mem.alloc((void **)&s->b3h, np * 8)) return LQT_ERR_NOMEM;
+        CK(cudaMemsetAsync(s->d6h, 0, np * 12, s->stream));
+        CK(cudaMemsetAsync(s->b3h, 0, np * 8, s->stream));
+        CK(launch_tensor_f16((const float *)s->d6, (const float *)s->b3, s->ntissue, s->d6h, s->b3h, s->stream));
     }
     // NaN everywhere (the tile padding included): plain steps until the first
     // macro-step boundary

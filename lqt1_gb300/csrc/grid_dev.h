@@ -1,5 +1,6 @@
 // grid_dev.h -- device view of a tissue grid simulation (k_grid.cuh, api_sim.cu).
 #pragma once
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -60,6 +61,10 @@ template <typename R> struct GridDev {
     const int32_t *plist;
     const int64_t *plist_n;
     int *serr;                     // bit 1 set when a substep's copy wait ran out
+    // FP16 copies of the tensor (xx yy | zz xy | xz yz: 3 half2 per voxel) and
+    // of its divergence (x y | z 0: 2 half2 per voxel) that the surrogate's
+    // V-only substep streams; null without a surrogate or on isotropic grids
+    const __half2 *d6h, *b3h;
 };
 
 // Voxels per tile of the staged substep kernel; the per-voxel arrays it

@@ -219,6 +219,34 @@ inline unsigned grid_list_blocks(int64_t ntissue)
 // read only where the macro-step kernel flagged that it can change.
 constexpr int kSubU = 2;
 
+// The surrogate substep's tensor rows in FP16 (3 half2 of the tensor, 2 of
+// the divergence per voxel; 2D reads the first 2 and 1): streaming loads,
+// widened to FP32 pairs.
+template <int DIM>
+__device__ __forceinline__ void sub_tensor_f16(const __half2 *d, const __half2 *b, float2 (&q)[5])
+{
+#pragma unroll
+    for (int i = 0; i < (DIM == 3 ? 3 : 2); ++i) q[i] = __half22float2(__ldcs(d + i));
+#pragma unroll
+    for (int i = 0; i < (DIM == 3 ? 2 : 1); ++i) q[3 + i] = __half22float2(__ldcs(b + i));
+}
+
+template <int DIM> __device__ __forceinline__ void sub_tensor_unpack(const float2 (&q)[5], float *Dt, float *Bt)
+{
+#pragma unroll
+    for (int i = 0; i < 6; ++i) Dt[i] = 0.f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) Bt[i] = 0.f;
+#pragma unroll
+    for (int i = 0; i < (DIM == 3 ? 3 : 2); ++i) {
+        Dt[2 * i] = q[i].x;
+        Dt[2 * i + 1] = q[i].y;
+    }
+    Bt[0] = q[3].x;
+    Bt[1] = q[3].y;
+    if (DIM == 3) Bt[2] = q[4].x;
+}
+
 template <int DIM>
 __device__ __forceinline__ float sub_du(const GridDev<float> &gd, const float *__restrict__ V, int64_t g, int64_t k,
                                         float vc, const float *Dt, const float *Bt)
@@ -248,7 +276,7 @@ template <int DIM, int MINB>
 __global__ void __launch_bounds__(256, MINB) k_sur_substep(GridDev<float> gd, float dt, int cur)
 {
     const int64_t k0 = blockIdx.x * (int64_t)(blockDim.x * kSubU) + threadIdx.x;
-    const bool aniso = DIM > 1 && gd.d6;
+    const bool aniso = DIM > 1 && gd.d6 && gd.d6h;
     float r[kSubU], Dt[kSubU][6], Bt[kSubU][3];
     int64_t g[kSubU];
     uint8_t ctl[kSubU], fl[kSubU];
@@ -266,16 +294,11 @@ __global__ void __launch_bounds__(256, MINB) k_sur_substep(GridDev<float> gd, fl
 #pragma unroll
         for (int i = 0; i < 3; ++i) Bt[u][i] = 0.f;
         if (aniso && on[u]) {
-            // streamed once per step: evict-first, the L2 is for the V rows
-            const float2 *d2 = reinterpret_cast<const float2 *>(gd.d6 + 6 * k);   // 24-byte rows: 8-byte aligned
-#pragma unroll
-            for (int i = 0; i < (DIM == 3 ? 3 : 2); ++i) {
-                const float2 q = __ldcs(d2 + i);
-                Dt[u][2 * i] = q.x;
-                Dt[u][2 * i + 1] = q.y;
-            }
-#pragma unroll
-            for (int i = 0; i < (DIM == 3 ? 3 : 2); ++i) Bt[u][i] = __ldcs(gd.b3 + 3 * k + i);
+            // the FP16 copies, streamed once per step: evict-first, the L2 is
+            // for the V rows
+            float2 q[5];
+            sub_tensor_f16<DIM>(gd.d6h + 3 * k, gd.b3h + 2 * k, q);
+            sub_tensor_unpack<DIM>(q, Dt[u], Bt[u]);
         }
     }
     bool any = false;

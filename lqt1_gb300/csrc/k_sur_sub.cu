@@ -15,13 +15,13 @@ namespace {
 constexpr uint32_t kSubWaitLimit = 1u << 22;   // bounded mbarrier polls per tile
 
 // One tile's rows, in the order of the copies: the macro step's ionic rate,
-// the dense index, the tensor (6 per voxel), its divergence (3 per voxel), the
-// control byte and the detector flag.
+// the dense index, the FP16 tensor (3 half2 per voxel), its FP16 divergence
+// (2 half2 per voxel), the control byte and the detector flag.
 struct __align__(16) SubStage {
     float rate[kSubTile];
     int32_t gidx[kSubTile];
-    float d6[kSubTile * 6];
-    float b3[kSubTile * 3];
+    __half2 d6[kSubTile * 3];
+    __half2 b3[kSubTile * 2];
     uint8_t ctl[kSubTile];
     uint8_t flag[kSubTile];
 };
@@ -36,11 +36,11 @@ static_assert(sizeof(SubStage) % 16 == 0 && offsetof(SubStage, gidx) % 16 == 0 &
 __device__ __forceinline__ void sub_issue(SubStage &sg, uint64_t *bar, const GridDev<float> &gd, int64_t k0, bool det)
 {
     constexpr uint32_t n = kSubTile;
-    tc::mbar_expect_tx(bar, n * (4 + 4 + 24 + 12 + 1) + (det ? n : 0));
+    tc::mbar_expect_tx(bar, n * (4 + 4 + 12 + 8 + 1) + (det ? n : 0));
     tc::bulk_g2s(sg.rate, gd.srate + k0, n * 4, bar);
     tc::bulk_g2s(sg.gidx, gd.gidx + k0, n * 4, bar);
-    tc::bulk_g2s(sg.d6, gd.d6 + 6 * k0, n * 24, bar);
-    tc::bulk_g2s(sg.b3, gd.b3 + 3 * k0, n * 12, bar);
+    tc::bulk_g2s(sg.d6, gd.d6h + 3 * k0, n * 12, bar);
+    tc::bulk_g2s(sg.b3, gd.b3h + 2 * k0, n * 8, bar);
     tc::bulk_g2s(sg.ctl, gd.ctl + k0, n, bar);
     if (det) tc::bulk_g2s(sg.flag, gd.sdflag + k0, n, bar);
 }
@@ -92,11 +92,13 @@ __global__ void __launch_bounds__(kSubTile, MINB) k_sur_substep_tile(GridDev<flo
         const float r = sg.rate[t];
         if (k < gd.ntissue && r == r) {
             const int64_t g = sg.gidx[t];
+            float2 q[5];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) q[i] = __half22float2(sg.d6[3 * t + i]);
+#pragma unroll
+            for (int i = 0; i < 2; ++i) q[3 + i] = __half22float2(sg.b3[2 * t + i]);
             float Dt[6], Bt[3];
-#pragma unroll
-            for (int i = 0; i < 6; ++i) Dt[i] = sg.d6[6 * t + i];
-#pragma unroll
-            for (int i = 0; i < 3; ++i) Bt[i] = sg.b3[3 * t + i];
+            sub_tensor_unpack<DIM>(q, Dt, Bt);
             const float vc = V[g];
             const float du = sub_du<DIM>(gd, V, g, k, vc, Dt, Bt);
             const float ist = grid_stim(gd, ck, sg.ctl[t], k);
@@ -161,8 +163,9 @@ cudaError_t launch_sur_substep(const GridDev<float> &gd, double dt, int cur, int
     if (gd.ntissue <= 0) return cudaSuccess;
     const bool tile = variant >= 100;
     const int minb = tile ? variant - 100 : variant;
-    if (tile && dim >= 2 && al16(gd.d6) && al16(gd.b3) && al16(gd.srate) && al16(gd.gidx) && al16(gd.ctl) &&
-        gd.serr && (!gd.det || al16(gd.sdflag))) {
+    if (dim >= 2 && gd.d6 && !(gd.d6h && gd.b3h)) return cudaErrorInvalidValue;   // FP16 tensor copies missing
+    if (tile && dim >= 2 && gd.d6 && al16(gd.d6h) && al16(gd.b3h) && al16(gd.srate) && al16(gd.gidx) &&
+        al16(gd.ctl) && gd.serr && (!gd.det || al16(gd.sdflag))) {
         if (dim == 2) {
             if (minb == 8) return launch_tile<2, 8>(gd, dt, cur, st);
             if (minb == 6) return launch_tile<2, 6>(gd, dt, cur, st);

@@ -1,6 +1,7 @@
 // k_util.cu -- state conversion between the reference's per-cell order
 // (40 doubles, TPORd::outputAllStates order, SingleCell/TPORd.cc:200-252) and
 // the device structure of arrays.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -129,6 +130,29 @@ cudaError_t launch_sample_v(const R *vg, const uint8_t *tissue, int32_t nx, int3
     k_sample_v<R><<<grid_for(n, 256), 256, 0, st>>>(vg, tissue, nx, ny, nz, stride, sx, sy, out);
     return cudaGetLastError();
 }
+// FP16 copies of the FP32 tensor rows (6 per voxel) and divergence rows (3
+// per voxel, padded to 4) for the surrogate's substep.
+__global__ void k_tensor_f16(const float *__restrict__ d6, const float *__restrict__ b3, int64_t n,
+                             __half2 *__restrict__ d6h, __half2 *__restrict__ b3h)
+{
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const float *d = d6 + 6 * k, *b = b3 + 3 * k;
+        d6h[3 * k + 0] = __floats2half2_rn(d[0], d[1]);
+        d6h[3 * k + 1] = __floats2half2_rn(d[2], d[3]);
+        d6h[3 * k + 2] = __floats2half2_rn(d[4], d[5]);
+        b3h[2 * k + 0] = __floats2half2_rn(b[0], b[1]);
+        b3h[2 * k + 1] = __floats2half2_rn(b[2], 0.f);
+    }
+}
+
+cudaError_t launch_tensor_f16(const float *d6, const float *b3, int64_t n, __half2 *d6h, __half2 *b3h,
+                              cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    k_tensor_f16<<<grid_for(n, 256), 256, 0, st>>>(d6, b3, n, d6h, b3h);
+    return cudaGetLastError();
+}
+
 template cudaError_t launch_sample_v<float>(const float *, const uint8_t *, int32_t, int32_t, int32_t, int32_t, int64_t,
                                             int64_t, double *, cudaStream_t);
 template cudaError_t launch_sample_v<double>(const double *, const uint8_t *, int32_t, int32_t, int32_t, int32_t,

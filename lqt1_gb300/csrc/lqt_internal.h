@@ -1,5 +1,6 @@
 // lqt_internal.h -- structures shared by the host API (api.cu) and kernels.
 #pragma once
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -101,6 +102,8 @@ namespace lqt {
 template <typename R, typename T>
 cudaError_t launch_gather_v(const R *vg, const int32_t *gidx, T *out, int64_t n, cudaStream_t st);
 template <typename R> cudaError_t launch_scatter_v(const R *v, const int32_t *gidx, R *vg, int64_t n, cudaStream_t st);
+cudaError_t launch_tensor_f16(const float *d6, const float *b3, int64_t n, __half2 *d6h, __half2 *b3h,
+                              cudaStream_t st);
 template <typename R>
 cudaError_t launch_sample_v(const R *vg, const uint8_t *tissue, int32_t nx, int32_t ny, int32_t nz, int32_t stride,
                             int64_t sx, int64_t sy, double *out, cudaStream_t st);
