@@ -95,9 +95,12 @@ struct lqt_sim {
     int *sur_err = nullptr;
     int64_t sur_launches = 0;
     // asynchronous V read-back: two device slots, a copy stream, events
+    // asynchronous V read-back: two device slots; each copy is split over
+    // kCopyStreams streams so that several copy engines share the host link
+    static constexpr int kCopyStreams = 4;
     void *vslot[2] = {nullptr, nullptr};
-    cudaStream_t copy_stream = nullptr;
-    cudaEvent_t gathered[2] = {nullptr, nullptr}, copied[2] = {nullptr, nullptr};
+    cudaStream_t copy_stream[kCopyStreams] = {};
+    cudaEvent_t gathered[2] = {nullptr, nullptr}, copied[2][kCopyStreams] = {};
     int vslot_next = 0;
     // output sampling: tissue mask of the dense grid, lattice buffer
     uint8_t *tmask = nullptr;
@@ -110,12 +113,15 @@ struct lqt_sim {
 
     ~lqt_sim()
     {
-        if (copy_stream) cudaStreamSynchronize(copy_stream);
+        for (cudaStream_t c : copy_stream)
+            if (c) cudaStreamSynchronize(c);
         for (int i = 0; i < 2; ++i) {
             if (gathered[i]) cudaEventDestroy(gathered[i]);
-            if (copied[i]) cudaEventDestroy(copied[i]);
+            for (cudaEvent_t e : copied[i])
+                if (e) cudaEventDestroy(e);
         }
-        if (copy_stream) cudaStreamDestroy(copy_stream);
+        for (cudaStream_t c : copy_stream)
+            if (c) cudaStreamDestroy(c);
         if (graph) cudaGraphExecDestroy(graph);
         if (own_stream && stream) cudaStreamDestroy(stream);
     }
@@ -816,13 +822,16 @@ int lqt_sim_get_v_async(lqt_sim *s, void *v_host, int as_double)
     if (!s || !v_host) return fail(LQT_ERR_INVALID, "lqt_sim_get_v_async: NULL");
     const int64_t n = s->ntissue;
     const size_t esz = as_double ? 8 : 4;
-    if (!s->copy_stream) {
+    constexpr int nc = lqt_sim::kCopyStreams;
+    if (!s->copy_stream[0]) {
         if (s->mem.alloc(&s->vslot[0], n * 8) || s->mem.alloc(&s->vslot[1], n * 8)) return LQT_ERR_NOMEM;
-        CK(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
+        for (int c = 0; c < nc; ++c) CK(cudaStreamCreateWithFlags(&s->copy_stream[c], cudaStreamNonBlocking));
         for (int i = 0; i < 2; ++i) {
             CK(cudaEventCreateWithFlags(&s->gathered[i], cudaEventDisableTiming));
-            CK(cudaEventCreateWithFlags(&s->copied[i], cudaEventDisableTiming));
-            CK(cudaEventRecord(s->copied[i], s->copy_stream));
+            for (int c = 0; c < nc; ++c) {
+                CK(cudaEventCreateWithFlags(&s->copied[i][c], cudaEventDisableTiming));
+                CK(cudaEventRecord(s->copied[i][c], s->copy_stream[c]));
+            }
         }
     }
     const int k = s->vslot_next;
@@ -830,7 +839,7 @@ int lqt_sim_get_v_async(lqt_sim *s, void *v_host, int as_double)
     void *slot = s->vslot[k];
     const int32_t *gi = s->dim > 1 ? s->gidx : nullptr;
     // the slot's previous copy must be done before the gather overwrites it
-    CK(cudaStreamWaitEvent(s->stream, s->copied[k], 0));
+    for (int c = 0; c < nc; ++c) CK(cudaStreamWaitEvent(s->stream, s->copied[k][c], 0));
     if (s->fp64()) {
         if (as_double) CK((launch_gather_v<double, double>((double *)s->vg[s->cur], gi, (double *)slot, n, s->stream)));
         else CK((launch_gather_v<double, float>((double *)s->vg[s->cur], gi, (float *)slot, n, s->stream)));
@@ -839,16 +848,25 @@ int lqt_sim_get_v_async(lqt_sim *s, void *v_host, int as_double)
         else CK((launch_gather_v<float, float>((float *)s->vg[s->cur], gi, (float *)slot, n, s->stream)));
     }
     CK(cudaEventRecord(s->gathered[k], s->stream));
-    CK(cudaStreamWaitEvent(s->copy_stream, s->gathered[k], 0));
-    CK(cudaMemcpyAsync(v_host, slot, n * esz, cudaMemcpyDeviceToHost, s->copy_stream));
-    CK(cudaEventRecord(s->copied[k], s->copy_stream));
+    // nc chunks of whole 256-byte blocks (the last takes the rest), one per stream
+    const size_t bytes = (size_t)n * esz;
+    const size_t chunk = (bytes / nc + 255) / 256 * 256;
+    for (int c = 0; c < nc; ++c) {
+        const size_t off = std::min(bytes, c * chunk);
+        const size_t len = std::min(bytes, off + chunk) - off;
+        CK(cudaStreamWaitEvent(s->copy_stream[c], s->gathered[k], 0));
+        if (len) CK(cudaMemcpyAsync((char *)v_host + off, (const char *)slot + off, len, cudaMemcpyDeviceToHost,
+                                    s->copy_stream[c]));
+        CK(cudaEventRecord(s->copied[k][c], s->copy_stream[c]));
+    }
     return LQT_OK;
 }
 
 int lqt_sim_wait_v(lqt_sim *s)
 {
     if (!s) return fail(LQT_ERR_INVALID, "lqt_sim_wait_v: NULL");
-    if (s->copy_stream) CK(cudaStreamSynchronize(s->copy_stream));
+    for (cudaStream_t c : s->copy_stream)
+        if (c) CK(cudaStreamSynchronize(c));
     return LQT_OK;
 }
 
