@@ -240,9 +240,18 @@ def fit_norm(X, D, nsample=500_000, seed=0):
     return in_mean, in_scale, out_scale
 
 
+# Pairs whose V lies in this range (mV) are repolarisation (phase 3) states:
+# the upstroke foot and the notch are outside the surrogate's |dV/dt| window.
+PHASE3_V = (-80.0, -20.0)
+
+
 def train(mlp: Mlp, X, D, *, epochs=4, batch=8192, lr=2e-3, lr_min=1e-4, holdout=0.01, seed=0, log_every=500,
-          log=print):
+          oversample=1, log=print):
     """Adam on shuffled mini-batches with a cosine learning-rate schedule.
+    oversample > 1 repeats the training split's phase-3 pairs (V in
+    PHASE3_V) that many times per epoch: they are a few percent of the pairs,
+    and a small bias of their correction accumulates over the ~100 macro steps
+    of repolarisation into the APD.  The held-out tail is never repeated.
     Returns per-state validation RMSE (physical units) and the loss history."""
     import math
 
@@ -254,12 +263,19 @@ def train(mlp: Mlp, X, D, *, epochs=4, batch=8192, lr=2e-3, lr_min=1e-4, holdout
     xb = torch.empty((batch, IN), dtype=torch.bfloat16, device="cuda")
     t = torch.empty((batch, OUT), dtype=torch.float32, device="cuda")
     g = torch.Generator(device="cuda").manual_seed(seed)
-    steps = epochs * (ntr // batch)
+    tr_idx = torch.arange(ntr, device="cuda")
+    if oversample > 1:
+        v = X[:ntr, 0]
+        sel = torch.nonzero((v > PHASE3_V[0]) & (v < PHASE3_V[1])).squeeze(1)
+        tr_idx = torch.cat([tr_idx, sel.repeat(oversample - 1)])
+        log(f"phase-3 pairs {int(sel.numel())} of {ntr}, repeated x{oversample}")
+    nep = tr_idx.numel() // batch
+    steps = epochs * nep
     hist = []
     k = 0
     for ep in range(epochs):
-        perm = torch.randperm(ntr, device="cuda", generator=g)
-        for b in range(ntr // batch):
+        perm = tr_idx[torch.randperm(tr_idx.numel(), device="cuda", generator=g)]
+        for b in range(nep):
             idx = perm[b * batch:(b + 1) * batch]
             N.check(L.lqt_sur_prepare(mlp._h, X.data_ptr(), D.data_ptr(), idx.data_ptr(), batch, xb.data_ptr(),
                                       t.data_ptr()), "lqt_sur_prepare")
@@ -293,6 +309,37 @@ def validate(mlp: Mlp, Xv, Dv, out_scale=None):
     return dict(rmse=rmse, zero_rmse=base, n=n)
 
 
+def validate_tissue(mlp: Mlp, *, n=64, t_end=600.0, dvdt_max=1.0, vstep_max=0.3, ref=None):
+    """APD90 error of the surrogate form against the FP64 form on a
+    validation tissue that the accuracy tests do not use: an n x n sheet at
+    0.15 mm (endo/M/epi bands, S1 on one edge, one beat) with the model GKs
+    x0.7, PCa x1.6, GKs-ISO x1.2.  Returns (mean signed error, max |error|,
+    the FP64 result for reuse)."""
+    from . import geometry
+    from .sim import Sim
+    sh = geometry.sheet(n, n, s1_cols=3)
+    m = N.model("baseline", gks_scale=0.7, pca_scale=1.6, gks_iso_scale=1.2)
+
+    def run(prec, net):
+        sim = Sim(sh.types, 0.15, precision=prec, model=m)
+        sim.set_protocol(bcl=1000.0, s1_mask=sh.s1_mask, s1_start=0.0, s1_duration=2.0, s1_strength=-52.0,
+                         s1_beats=1)
+        if net is not None:
+            sim.set_surrogate(net, dvdt_max=dvdt_max, vstep_max=vstep_max)
+        sim.step(int(round(t_end / 0.02)))
+        d = sim.detect()
+        sim.close()
+        return d["apd90"]
+    if ref is None:
+        ref = run(N.FP64, None)
+    a = run(N.MIXED, mlp)
+    ok = (a > 0) & (ref > 0)
+    e = (a - ref)[ok]
+    if e.size == 0 or ok.sum() < 0.99 * (ref > 0).sum():
+        return float("inf"), float("inf"), ref
+    return float(e.mean()), float(np.abs(e).max()), ref
+
+
 DEFAULT_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "tpord_surrogate.npz")
 
 
@@ -318,12 +365,20 @@ def load(path: str | None = None, stream: int | None = None) -> Mlp:
 
 
 def train_default(out=DEFAULT_WEIGHTS, *, ncells=65536, cap=20_000_000, prob=None, epochs=20, batch=8192,
-                  lr=2e-3, seed=1, tissue=0, nsub=10, log=print):
+                  lr=2e-3, seed=1, tissue=0, nsub=10, oversample=1, select=4, log=print):
     """Generate the pairs (paced single cells with the sweep's parameter
     ranges, plus `tissue` pairs from 2D S1-S2 sheets), fit the normalisation,
-    train, validate, save.  The defaults reproduce the shipped network: macro
-    steps of 10 plain steps (0.2 ms), recording probability 0.001 * nsub
-    (about cap pairs from 6 beats of 65,536 cells), 20 epochs."""
+    train `select` networks (seeds seed, seed + 1, ...) on the same pairs,
+    keep the one whose APD90 on the validation tissue (validate_tissue) is
+    least biased against the FP64 form, save.  Networks with the same
+    per-pair loss differ in a small state-dependent bias that shifts every
+    cell's APD by up to ~0.5 ms; the squared loss does not see it, the
+    tissue does.  Defaults: macro steps of 10 plain steps (0.2 ms), recording
+    probability 0.001 * nsub (about cap pairs from 6 beats of 65,536 cells),
+    20 epochs, best of 4.  The shipped network came from this recipe with
+    one candidate and was kept after validation on held-out tissues; a rerun
+    is not bitwise reproducible (the pair generator's slot order depends on
+    atomics), so its candidates differ from it."""
     if prob is None:
         prob = 0.001 * nsub
     import time
@@ -343,17 +398,31 @@ def train_default(out=DEFAULT_WEIGHTS, *, ncells=65536, cap=20_000_000, prob=Non
     torch.cuda.synchronize()
     t1 = time.perf_counter()
     log(f"pairs {X.shape[0]} ({X.shape[0] - tissue if tissue else X.shape[0]} single-cell) in {t1 - t0:.1f} s")
-    m = Mlp(seed=seed)
-    m.nsub = nsub
     im, isc, osc = fit_norm(X, D)
-    m.set_norm(im, isc, osc)
-    m.set_bounds(fit_bounds(D, osc))
-    val, hist = train(m, X, D, epochs=epochs, batch=batch, lr=lr, seed=seed, log=log)
+    bounds = fit_bounds(D, osc)
+    best, ref, cand = None, None, []
+    for i in range(max(1, select)):
+        m = Mlp(seed=seed + i)
+        m.nsub = nsub
+        m.set_norm(im, isc, osc)
+        m.set_bounds(bounds)
+        val_i, hist_i = train(m, X, D, epochs=epochs, batch=batch, lr=lr, seed=seed + i, oversample=oversample,
+                              log=log)
+        bias, emax, ref = validate_tissue(m, ref=ref)
+        cand.append(dict(seed=seed + i, apd_bias_ms=bias, apd_max_ms=emax))
+        log(f"candidate seed {seed + i}: validation APD90 bias {bias:+.3f} ms, max {emax:.3f} ms")
+        if best is None or (abs(bias), emax) < (abs(best[1]), best[2]):
+            if best is not None:
+                best[0].close()
+            best = (m, bias, emax, val_i, hist_i, seed + i)
+        else:
+            m.close()
+    m, _, _, val, hist, seed_best = best
     torch.cuda.synchronize()
     t2 = time.perf_counter()
     rel = val["rmse"] / np.maximum(val["zero_rmse"], 1e-30)
     meta = dict(pairs=int(X.shape[0]), tissue_pairs=int(tissue), ncells=ncells, epochs=epochs, batch=batch, lr=lr,
-                seed=seed, dt=0.02, prob=prob,
+                seed=seed_best, data_seed=seed, dt=0.02, prob=prob, oversample_phase3=oversample, candidates=cand,
                 macro_steps=nsub, gen_s=t1 - t0, train_s=t2 - t1, loss_history=[(int(k), float(l)) for k, l in hist],
                 val_rmse=val["rmse"].tolist(), val_zero_rmse=val["zero_rmse"].tolist(), val_n=int(val["n"]),
                 state_names=STATE_NAMES)
@@ -384,9 +453,12 @@ def main():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--tissue", type=int, default=0, help="pairs from 2D S1-S2 sheets mixed in (0 = none)")
     ap.add_argument("--nsub", type=int, default=10, help="plain steps per macro step (divides 50)")
+    ap.add_argument("--oversample", type=int, default=1, help="repeats of the phase-3 pairs per epoch")
+    ap.add_argument("--select", type=int, default=4, help="networks trained; the least APD-biased is kept")
     a = ap.parse_args()
     train_default(a.out, ncells=a.cells, cap=a.pairs, prob=a.prob, epochs=a.epochs, batch=a.batch, lr=a.lr,
-                  seed=a.seed, tissue=a.tissue, nsub=a.nsub, log=lambda m: print(m, flush=True))
+                  seed=a.seed, tissue=a.tissue, nsub=a.nsub, oversample=a.oversample, select=a.select,
+                  log=lambda m: print(m, flush=True))
 
 
 if __name__ == "__main__":
