@@ -242,3 +242,49 @@ def test_substep_variants_bit_identical(lq, net, dim):
         for key in d0:
             np.testing.assert_array_equal(d[key], d0[key], err_msg=f"variant {var}: {key}")
         assert s == s0 and b == b0, var
+
+
+def test_macro_length_and_rejection_counters(lq, orc, net):
+    """The macro length follows the network unless overridden (it must divide
+    the 50-step graph span); each residual check's failures are counted: with
+    a vanishing network bound every offered voxel fails it and none is
+    accepted, and the voxels then take plain steps."""
+    st = orc.initial_state(-87.5)
+    om = orc.model("baseline", gks_scale=0.5, pca_scale=2.0, gks_iso_scale=1.5)
+    orc.cells_update(st, [orc.ENDO], om, dt=0.02, ist=np.array([-52.0]), nsteps=100)
+    orc.cells_update(st, [orc.ENDO], om, dt=0.02, nsteps=7400)
+    sh = lq.geometry.sheet(16, 16, s1_cols=1)
+    types = np.where(sh.types == 255, 255, orc.ENDO).astype(np.uint8)
+    m = lq.model("baseline", gks_scale=0.5, pca_scale=2.0, gks_iso_scale=1.5)
+
+    def sim_with(**kw):
+        sim = lq.Sim(types, 0.15, precision=lq.MIXED, model=m)
+        sim.set_state(np.repeat(st, sim.n, 0))
+        sim.set_surrogate(net, **kw)
+        return sim
+
+    for bad in (7, 51, -2):
+        with pytest.raises(lq.LqtError):
+            sim_with(nsub=bad)
+    sim = sim_with(nsub=5)
+    sim.step(20)
+    s5 = sim.surrogate_stats()
+    assert s5["macro_steps"] == 4 and s5["accepted"] > 0
+    sim.close()
+    sim = sim_with()
+    sim.step(20)
+    assert sim.surrogate_stats()["macro_steps"] == 20 // net.nsub
+    assert sum(sim.surrogate_rejections().values()) == 0
+    sim.close()
+    sim = sim_with(kappa=1e-9)
+    sim.step(20)
+    s0 = sim.surrogate_stats()
+    rj = sim.surrogate_rejections()
+    assert s0["offered"] > 0 and s0["accepted"] == 0
+    assert rj["network_bound"] == s0["offered"]
+    plain = lq.Sim(types, 0.15, precision=lq.MIXED, model=m)
+    plain.set_state(np.repeat(st, plain.n, 0))
+    plain.step(20)
+    np.testing.assert_array_equal(sim.get_state(), plain.get_state())   # every voxel ran the plain step
+    sim.close()
+    plain.close()
