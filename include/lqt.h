@@ -539,9 +539,9 @@ int lqt_sur_prepare(lqt_mlp *m, const float *x_dev, const float *d_dev,
  * the caller and must outlive the attachment; its parameters are read at
  * every macro step. */
 typedef struct lqt_sur_config {
-    double dvdt_max;    /* mV/ms, e.g. 1 */
+    double dvdt_max;    /* mV/ms, e.g. 1.5 */
     double kappa;       /* multiplier of the network's residual bounds, e.g. 1.5 */
-    double vstep_max;   /* mV per macro step, e.g. 0.3 */
+    double vstep_max;   /* mV per macro step, e.g. 0.4 */
     int32_t use_net;
     int32_t nsub;       /* plain steps per macro step; divides 50; 0 = 5 */
 } lqt_sur_config;

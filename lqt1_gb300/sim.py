@@ -160,7 +160,7 @@ class Sim:
         return VtkWriter(self, stride, nbuf)
 
     # ---- learned surrogate ---------------------------------------------------------
-    def set_surrogate(self, mlp=None, *, dvdt_max: float = 1.0, kappa: float = 1.5, vstep_max: float = 0.3,
+    def set_surrogate(self, mlp=None, *, dvdt_max: float = 1.5, kappa: float = 1.5, vstep_max: float = 0.4,
                       use_net: bool = True, nsub: int | None = None):
         """Attach a trained surrogate network (lqt1_gb300.surrogate.Mlp) or
         detach (None).  Mixed form only; see lqt_sim_set_surrogate.  The macro

@@ -365,7 +365,7 @@ def load(path: str | None = None, stream: int | None = None) -> Mlp:
 
 
 def train_default(out=DEFAULT_WEIGHTS, *, ncells=65536, cap=20_000_000, prob=None, epochs=20, batch=8192,
-                  lr=2e-3, seed=1, tissue=0, nsub=10, oversample=1, select=4, log=print):
+                  lr=2e-3, seed=1, tissue=0, nsub=10, oversample=4, select=4, log=print):
     """Generate the pairs (paced single cells with the sweep's parameter
     ranges, plus `tissue` pairs from 2D S1-S2 sheets), fit the normalisation,
     train `select` networks (seeds seed, seed + 1, ...) on the same pairs,
@@ -375,10 +375,11 @@ def train_default(out=DEFAULT_WEIGHTS, *, ncells=65536, cap=20_000_000, prob=Non
     cell's APD by up to ~0.5 ms; the squared loss does not see it, the
     tissue does.  Defaults: macro steps of 10 plain steps (0.2 ms), recording
     probability 0.001 * nsub (about cap pairs from 6 beats of 65,536 cells),
-    20 epochs, best of 4.  The shipped network came from this recipe with
-    one candidate and was kept after validation on held-out tissues; a rerun
-    is not bitwise reproducible (the pair generator's slot order depends on
-    atomics), so its candidates differ from it."""
+    phase-3 pairs repeated 4 times, 20 epochs, best of 4.  The shipped
+    network came from this recipe with one candidate and was selected by the
+    same validation among the networks trained so far (its file records
+    them); a rerun is not bitwise reproducible (the pair generator's slot
+    order depends on atomics), so its candidates differ from it."""
     if prob is None:
         prob = 0.001 * nsub
     import time
@@ -453,7 +454,7 @@ def main():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--tissue", type=int, default=0, help="pairs from 2D S1-S2 sheets mixed in (0 = none)")
     ap.add_argument("--nsub", type=int, default=10, help="plain steps per macro step (divides 50)")
-    ap.add_argument("--oversample", type=int, default=1, help="repeats of the phase-3 pairs per epoch")
+    ap.add_argument("--oversample", type=int, default=4, help="repeats of the phase-3 pairs per epoch")
     ap.add_argument("--select", type=int, default=4, help="networks trained; the least APD-biased is kept")
     a = ap.parse_args()
     train_default(a.out, ncells=a.cells, cap=a.pairs, prob=a.prob, epochs=a.epochs, batch=a.batch, lr=a.lr,
