@@ -322,10 +322,13 @@ def main():
     # copy stream that overlaps the next step, all copies complete inside the
     # timed region -- and the final state D2H.
     st_host = torch.empty((n, 40), dtype=torch.float64, pin_memory=True).numpy()
-    ring = 8                      # pinned host buffers; a buffer is reused after a wait
+    # pinned host buffers; a buffer is reused after a wait, and a wait drains
+    # every copy in flight (the GPU idles while the host waits on the newest
+    # one), so the ring is deep: 32 x 28 MB, one wait per 32 steps
+    ring = 32
     v_host = [torch.empty(n, dtype=torch.float32, pin_memory=True).numpy() for _ in range(ring)]
     sim.get_state(out=st_host)
-    k_e2e = max(10, min(args.steps, 5000))
+    k_e2e = max(10, args.steps)    # the same number of steps (a whole beat by default) as the headline
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     sim.set_state(st_host)

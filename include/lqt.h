@@ -296,10 +296,15 @@ int lqt_sim_set_electrodes(lqt_sim *s, int32_t n, const double *xyz_host,
                            int32_t every);
 /* V of every tissue voxel into a host buffer without waiting (the reference
  * copies V back every step, GPU3D.cu:1802): the gather into one of two device
- * slots runs on the simulation's stream, the copy on a second stream, so it
+ * slots runs on the simulation's stream, the copy on four copy streams, so it
  * overlaps the next steps.  The buffer (pinned memory for a true overlap) is
  * complete after lqt_sim_wait_v; a buffer must not be reused before that. */
 int lqt_sim_get_v_async(lqt_sim *s, void *v_host, int as_double);
+/* Waits for every read-back copy in flight.  The GPU idles while the host
+ * waits on the newest copy, so a caller that reads V back every step keeps
+ * a ring of buffers and waits once per ring (32 buffers: 0.31 ms per step of
+ * the 7.1M-voxel surrogate form, against 0.38 ms with a wait every 8 steps
+ * and 0.26 ms without read-back). */
 int lqt_sim_wait_v(lqt_sim *s);
 
 /* Samples recorded since the electrodes were set: [nsamples][n], and time. */
