@@ -317,7 +317,7 @@ def main():
                                                                     "oversample_phase3", "gen_and_train_s")}}
 
     # e2e through the C ABI with pinned host buffers: initial state H2D, then
-    # every step lqt_sim_step + a read-back of V to the host (the reference's
+    # every step lqt_sim_step_async + a read-back of V to the host (the reference's
     # host loop copies V back every step, GPU3D.cu:1802) -- asynchronous, on a
     # copy stream that overlaps the next step, all copies complete inside the
     # timed region -- and the final state D2H.
@@ -333,10 +333,11 @@ def main():
     t0 = time.perf_counter()
     sim.set_state(st_host)
     for i in range(k_e2e):
-        sim.step(1)
+        sim.step_async(1)
         if i % ring == 0 and i > 0:
             sim.wait_v()
         sim.get_v_async(v_host[i % ring])
+    sim.sync()
     sim.wait_v()
     sim.get_state(out=st_host)
     t_e2e = time.perf_counter() - t0

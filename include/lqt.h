@@ -279,8 +279,16 @@ int64_t lqt_sim_num_tissue(const lqt_sim *s);
 int lqt_sim_tissue_index(const lqt_sim *s, int64_t *grid_index_host);
 
 /* Advance nsteps of dt.  Simulated time accumulates as `time += dt` in FP64,
- * as the reference drivers do (OneD.cc:317). */
+ * as the reference drivers do (OneD.cc:317).  Returns when the steps have run
+ * on the device. */
 int lqt_sim_step(lqt_sim *s, int64_t nsteps);
+/* The same steps, enqueued on the simulation's stream without waiting: a host
+ * loop that issues one step at a time (with a read-back per step) keeps the
+ * device busy instead of paying a host round-trip per step.  Device errors
+ * surface at the next call that waits (lqt_sim_sync, lqt_sim_step, a read). */
+int lqt_sim_step_async(lqt_sim *s, int64_t nsteps);
+/* Waits for every step enqueued on the simulation's stream. */
+int lqt_sim_sync(lqt_sim *s);
 double lqt_sim_time(const lqt_sim *s);
 
 /* V of every tissue voxel (tissue order), as float or double. */

@@ -115,6 +115,8 @@ def lib():
         "lqt_sim_num_tissue": ([P], I64),
         "lqt_sim_tissue_index": ([P, P], I),
         "lqt_sim_step": ([P, I64], I),
+        "lqt_sim_step_async": ([P, I64], I),
+        "lqt_sim_sync": ([P], I),
         "lqt_sim_time": ([P], D),
         "lqt_sim_get_v": ([P, P, I], I),
         "lqt_sim_get_state": ([P, P], I),

@@ -754,9 +754,10 @@ int lqt_sim_set_protocol(lqt_sim *s, const lqt_protocol *q)
     return LQT_OK;
 }
 
-int lqt_sim_step(lqt_sim *s, int64_t nsteps)
+// Enqueue nsteps steps on the simulation's stream (graph chunks where they
+// fit, single steps elsewhere); the host does not wait for them.
+static int sim_advance(lqt_sim *s, int64_t nsteps)
 {
-    if (!s || nsteps < 0) return fail(LQT_ERR_INVALID, "lqt_sim_step: NULL handle or nsteps < 0");
     if (s->has_protocol && s->step + nsteps + kGraphChunk > s->win_horizon) {
         int rc = refresh_windows(s, s->step + nsteps + 200000);
         if (rc) return rc;
@@ -790,6 +791,27 @@ int lqt_sim_step(lqt_sim *s, int64_t nsteps)
         if (rc) return rc;
         --left;
     }
+    return LQT_OK;
+}
+
+int lqt_sim_step(lqt_sim *s, int64_t nsteps)
+{
+    if (!s || nsteps < 0) return fail(LQT_ERR_INVALID, "lqt_sim_step: NULL handle or nsteps < 0");
+    const int rc = sim_advance(s, nsteps);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(s->stream));
+    return LQT_OK;
+}
+
+int lqt_sim_step_async(lqt_sim *s, int64_t nsteps)
+{
+    if (!s || nsteps < 0) return fail(LQT_ERR_INVALID, "lqt_sim_step_async: NULL handle or nsteps < 0");
+    return sim_advance(s, nsteps);
+}
+
+int lqt_sim_sync(lqt_sim *s)
+{
+    if (!s) return fail(LQT_ERR_INVALID, "lqt_sim_sync: NULL handle");
     CK(cudaStreamSynchronize(s->stream));
     return LQT_OK;
 }

@@ -68,6 +68,14 @@ class Sim:
     def step(self, nsteps: int = 1):
         N.check(N.lib().lqt_sim_step(self._h, int(nsteps)), "lqt_sim_step")
 
+    def step_async(self, nsteps: int = 1):
+        """Enqueue nsteps steps without waiting for them (see lqt_sim_step_async)."""
+        N.check(N.lib().lqt_sim_step_async(self._h, int(nsteps)), "lqt_sim_step_async")
+
+    def sync(self):
+        """Wait for every enqueued step."""
+        N.check(N.lib().lqt_sim_sync(self._h), "lqt_sim_sync")
+
     @property
     def time(self) -> float:
         return float(N.lib().lqt_sim_time(self._h))

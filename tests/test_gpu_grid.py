@@ -194,3 +194,47 @@ def test_async_v_readback_matches_sync(lq):
     sim.get_v_async(b64)
     sim.wait_v()
     np.testing.assert_array_equal(b64, sim.get_v(as_double=True))
+
+
+def test_async_steps_match_synchronous_steps(lq):
+    """lqt_sim_step_async: single steps enqueued without waiting, each with a
+    V read-back into a ring of pinned buffers, give the same bits as
+    lqt_sim_step over the same steps; every read-back holds the V of its
+    step.  The surrogate is attached, so macro steps and substeps are among
+    the enqueued work."""
+    import torch
+    from lqt1_gb300 import surrogate as S
+    net = S.load()
+    v = lq.geometry.ventricle(nx=44, ny=44, nz=50, dx=0.2, a_out=4.0, c_out=8.0, wall=2.0, z_base=9.0,
+                              island_radius=1.5, stim_radius=1.2)
+    m = lq.model("baseline", gks_scale=0.5, pca_scale=2.0, gks_iso_scale=1.5)
+
+    def make():
+        sim = lq.Sim(v.types, 0.2, fibre=v.fibre, precision=lq.MIXED, model=m)
+        sim.set_protocol(bcl=800.0, s1_mask=v.s1_mask, s1_start=0.0, s1_duration=2.0, s1_strength=-52.0)
+        sim.set_surrogate(net)
+        sim.tune(4)
+        sim.substep_variant(5)
+        return sim
+    a, b = make(), make()
+    a.step(5)
+    b.step(5)
+    K, ring = 120, 16
+    bufs = [torch.empty(a.n, dtype=torch.float32, pin_memory=True).numpy() for _ in range(ring)]
+    ref = []
+    for i in range(K):
+        a.step_async(1)
+        if i % ring == 0 and i > 0:
+            a.wait_v()
+            for j in range(ring):
+                np.testing.assert_array_equal(bufs[j], ref[i - ring + j])
+        a.get_v_async(bufs[i % ring])
+        b.step(1)
+        ref.append(b.get_v())
+    a.sync()
+    a.wait_v()
+    np.testing.assert_array_equal(a.get_state(), b.get_state())
+    assert a.surrogate_stats() == b.surrogate_stats()
+    assert a.time == b.time
+    a.close()
+    b.close()
