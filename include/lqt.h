@@ -387,7 +387,9 @@ int lqt_ecg_grid_noalloc(const float *v_grid_dev, int32_t nx, int32_t ny,
                          int32_t nel, double *phi_dev, void *stream);
 
 /* Blow-up detector: count of voxels with NaN or V outside [vmin_ok, vmax_ok]
- * since the last call (GPU3D.cu:1796-1829 does this scan on the host). */
+ * since the last call (GPU3D.cu:1796-1829 does this scan on the host);
+ * LQT_ERR_NUMERIC when it is not zero.  Also LQT_ERR_CUDA when a surrogate
+ * substep's tile-copy wait ran out (some voxels missed a substep). */
 int lqt_sim_check(lqt_sim *s, int64_t *n_bad);
 
 /* Binary checkpoint: header + version + per-state arrays. */

@@ -954,6 +954,7 @@ int lqt_sim_set_state(lqt_sim *s, const double *state_host)
     c.time = s->time;
     c.time_f = (float)s->time;
     c.s1_cycle_ok = 1;
+    CK(cudaStreamSynchronize(s->stream));    // steps enqueued without waiting read the clock
     CK(cudaMemcpy(s->clk, &c, sizeof(c), cudaMemcpyHostToDevice));
     return LQT_OK;
 }
@@ -993,6 +994,7 @@ int lqt_sim_get_ecg(lqt_sim *s, int64_t max_samples, double *phi, double *t, int
     if (!s) return fail(LQT_ERR_INVALID, "lqt_sim_get_ecg: NULL");
     if (s->nel == 0) return fail(LQT_ERR_STATE, "lqt_sim_get_ecg: no electrodes set");
     int64_t cnt = 0;
+    CK(cudaStreamSynchronize(s->stream));
     CK(cudaMemcpy(&cnt, s->ecg_count, 8, cudaMemcpyDeviceToHost));
     if (nsamples) *nsamples = cnt;
     const int64_t m = std::min(cnt, max_samples);
@@ -1011,6 +1013,7 @@ int lqt_sim_get_detect(lqt_sim *s, float *t_act, float *apd90, uint8_t *ead)
     if (!s->det) return fail(LQT_ERR_STATE, "lqt_sim_get_detect: created with detect = 0");
     const int64_t n = s->ntissue;
     std::vector<float4> d(n);
+    CK(cudaStreamSynchronize(s->stream));
     CK(cudaMemcpy(d.data(), s->det, n * sizeof(float4), cudaMemcpyDeviceToHost));
     for (int64_t k = 0; k < n; ++k) {
         uint32_t bits;
@@ -1123,9 +1126,17 @@ int lqt_sim_check(lqt_sim *s, int64_t *n_bad)
 {
     if (!s || !n_bad) return fail(LQT_ERR_INVALID, "lqt_sim_check: NULL");
     unsigned long long v = 0;
+    CK(cudaStreamSynchronize(s->stream));
     CK(cudaMemcpy(&v, s->nbad, sizeof(v), cudaMemcpyDeviceToHost));
     CK(cudaMemset(s->nbad, 0, sizeof(v)));
     *n_bad = (int64_t)v;
+    if (s->sur_err) {
+        int err = 0;
+        CK(cudaMemcpy(&err, s->sur_err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err & 2)
+            return fail(LQT_ERR_CUDA, "lqt_sim_check: a surrogate substep's tile-copy wait ran out; voxels missed "
+                                      "that substep and the run is not valid");
+    }
     return v ? LQT_ERR_NUMERIC : LQT_OK;
 }
 
