@@ -365,7 +365,7 @@ def load(path: str | None = None, stream: int | None = None) -> Mlp:
 
 
 def train_default(out=DEFAULT_WEIGHTS, *, ncells=65536, cap=20_000_000, prob=None, epochs=20, batch=8192,
-                  lr=2e-3, seed=1, tissue=0, nsub=10, oversample=4, select=4, log=print):
+                  lr=2e-3, seed=1, tissue=0, nsub=10, oversample=4, select=4, jitter=0.3, log=print):
     """Generate the pairs (paced single cells with the sweep's parameter
     ranges, plus `tissue` pairs from 2D S1-S2 sheets), fit the normalisation,
     train `select` networks (seeds seed, seed + 1, ...) on the same pairs,
@@ -386,7 +386,8 @@ def train_default(out=DEFAULT_WEIGHTS, *, ncells=65536, cap=20_000_000, prob=Non
 
     import torch
     t0 = time.perf_counter()
-    X, D = generate(ncells=ncells, cap=cap - tissue, prob=prob * (cap - tissue) / cap, seed=seed, nsub=nsub)
+    X, D = generate(ncells=ncells, cap=cap - tissue, prob=prob * (cap - tissue) / cap, seed=seed, nsub=nsub,
+                    jitter=jitter)
     if tissue > 0:
         Xt, Dt = tissue_pairs(tissue, seed=seed + 6, nsub=nsub, log=log)
         X, D = torch.cat([X, Xt]), torch.cat([D, Dt])
@@ -423,7 +424,8 @@ def train_default(out=DEFAULT_WEIGHTS, *, ncells=65536, cap=20_000_000, prob=Non
     t2 = time.perf_counter()
     rel = val["rmse"] / np.maximum(val["zero_rmse"], 1e-30)
     meta = dict(pairs=int(X.shape[0]), tissue_pairs=int(tissue), ncells=ncells, epochs=epochs, batch=batch, lr=lr,
-                seed=seed_best, data_seed=seed, dt=0.02, prob=prob, oversample_phase3=oversample, candidates=cand,
+                seed=seed_best, data_seed=seed, dt=0.02, prob=prob, jitter=jitter, oversample_phase3=oversample,
+                candidates=cand,
                 macro_steps=nsub, gen_s=t1 - t0, train_s=t2 - t1, loss_history=[(int(k), float(l)) for k, l in hist],
                 val_rmse=val["rmse"].tolist(), val_zero_rmse=val["zero_rmse"].tolist(), val_n=int(val["n"]),
                 state_names=STATE_NAMES)
