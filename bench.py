@@ -88,10 +88,11 @@ class ClockSampler:
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, device: int):
+    def __init__(self, device: int, path: str | None = None):
+        import tempfile
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{device}.csv")
+        self.path = path or os.path.join(tempfile.gettempdir(), f"lqt_bench_clocks_rank{device}.csv")
 
     def __enter__(self):
         try:
@@ -204,6 +205,7 @@ def main():
     ap.add_argument("--workload", default="ventricle3d", choices=["ventricle3d", "ventricle3d_small", "sheet2d"])
     ap.add_argument("--prerun", type=int, default=0, help="untimed steps before the timed region (setup)")
     ap.add_argument("--weights", default=None, help="surrogate network file (default: the shipped network)")
+    ap.add_argument("--clocks-csv", default=None, help="where to keep the raw nvidia-smi samples (default: temp dir)")
     ap.add_argument("--sur-dvdt-max", type=float, default=1.5, help="surrogate eligibility: |dV/dt| bound, mV/ms")
     ap.add_argument("--sur-vstep-max", type=float, default=0.4, help="surrogate residual check: ionic dV per macro step")
     ap.add_argument("--fp64-steps", type=int, default=10)
@@ -288,7 +290,7 @@ def main():
     sub_variant, sub_ms = sim.substep_variant(-1, timings=True)   # and of the V-only substep
     sim.step(args.warmup)
     sim.surrogate_stats(reset=True)
-    with ClockSampler(dev) as clk:
+    with ClockSampler(dev, args.clocks_csv) as clk:
         ms = timed(sim, args.steps)
     value = world * n * args.steps / (ms / 1e3)
     nbad = sim.check()
