@@ -206,6 +206,8 @@ def main():
     ap.add_argument("--prerun", type=int, default=0, help="untimed steps before the timed region (setup)")
     ap.add_argument("--weights", default=None, help="surrogate network file (default: the shipped network)")
     ap.add_argument("--clocks-csv", default=None, help="where to keep the raw nvidia-smi samples (default: temp dir)")
+    ap.add_argument("--substep-variant", type=int, default=-1,
+                    help="force the surrogate substep kernel (5/6/8 direct, 105/106/108 staged; -1 = autotune)")
     ap.add_argument("--sur-dvdt-max", type=float, default=1.5, help="surrogate eligibility: |dV/dt| bound, mV/ms")
     ap.add_argument("--sur-vstep-max", type=float, default=0.4, help="surrogate residual check: ionic dV per macro step")
     ap.add_argument("--fp64-steps", type=int, default=10)
@@ -286,6 +288,8 @@ def main():
     sim = make_sim(lq.MIXED, True)
     n = sim.n
     sim.step(args.prerun)
+    if args.substep_variant >= 0:
+        sim.substep_variant(args.substep_variant)
     variant, tune_ms = sim.tune(-1)          # occupancy variant of the plain step kernel
     sub_variant, sub_ms = sim.substep_variant(-1, timings=True)   # and of the V-only substep
     sim.step(args.warmup)
