@@ -573,6 +573,13 @@ int lqt_sim_surrogate_stats(lqt_sim *s, int64_t *macro_steps, int64_t *offered,
  * bound, [1] a gate outside [0, 1] or not finite, [2] a concentration not
  * positive, [3] the ionic V change beyond vstep_max. */
 int lqt_sim_surrogate_rejections(lqt_sim *s, int64_t *counts);
+/* Test of the failure path, no use in production runs: skip_first_copy = 1
+ * makes the staged substep kernel (variants 105/106/108) leave out the first
+ * tile's copies of every CTA, so that tile's bounded mbarrier wait runs out;
+ * wait_limit sets the polls per wait (0 = the default).  The CTA then sets bit
+ * 1 of the surrogate error word, lets its copies in flight land and returns;
+ * lqt_sim_check reports it and the context stays usable.  (0, 0) restores. */
+int lqt_sim_set_wait_test(lqt_sim *s, int32_t skip_first_copy, uint32_t wait_limit);
 
 /* ======================================================================== *
  *  Synthetic geometries (seeded).  The reference reads its geometry from

@@ -79,6 +79,8 @@ struct lqt_sim {
     int minb = 2;
     int sub_minb = 5;               // V-only substep variant (kSubVariants)
     bool sub_forced = false;        // set by lqt_sim_substep_variant: the autotuner keeps it
+    int32_t sub_skip_copy = 0;      // failure-path test (lqt_sim_set_wait_test)
+    uint32_t sub_wait_limit = 0;
     float sub_tune_ms[kSubNVariants] = {};   // last autotune: mean ms per substep variant
     bool tuned = false;
     float tune_ms[4] = {0, 0, 0, 0};
@@ -178,6 +180,8 @@ struct lqt_sim {
         g.serr = in_macro ? sur_err : nullptr;
         g.d6h = in_macro ? d6h : nullptr;
         g.b3h = in_macro ? b3h : nullptr;
+        g.sub_skip_copy = sub_skip_copy;
+        g.sub_wait_limit = sub_wait_limit;
         return g;
     }
     double diso = 0.154;
@@ -1212,6 +1216,17 @@ int lqt_sim_set_surrogate(lqt_sim *s, lqt_mlp *m, const lqt_sur_config *cfg)
     s->sur_cfg = *cfg;
     s->sur_nsub = sur_nsub_or_default(cfg->nsub);
     s->plist_valid = false;
+    s->graph_valid = false;
+    return LQT_OK;
+}
+
+int lqt_sim_set_wait_test(lqt_sim *s, int32_t skip_first_copy, uint32_t wait_limit)
+{
+    if (!s || (skip_first_copy != 0 && skip_first_copy != 1))
+        return fail(LQT_ERR_INVALID, "lqt_sim_set_wait_test: NULL handle or skip_first_copy not 0/1");
+    CK(cudaStreamSynchronize(s->stream));
+    s->sub_skip_copy = skip_first_copy;
+    s->sub_wait_limit = wait_limit;
     s->graph_valid = false;
     return LQT_OK;
 }

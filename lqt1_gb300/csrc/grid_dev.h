@@ -65,6 +65,11 @@ template <typename R> struct GridDev {
     // of its divergence (x y | z 0: 2 half2 per voxel) that the surrogate's
     // V-only substep streams; null without a surrogate or on isotropic grids
     const __half2 *d6h, *b3h;
+    // test of the failure path (lqt_sim_set_wait_test): 1 = the staged
+    // substep leaves out the first tile's copies of every CTA, so that wait
+    // runs out; wait_limit = polls per wait (0 = the default limit)
+    int32_t sub_skip_copy;
+    uint32_t sub_wait_limit;
 };
 
 // Voxels per tile of the staged substep kernel; the per-voxel arrays it

@@ -53,7 +53,9 @@ __device__ __forceinline__ void sub_issue(SubStage &sg, uint64_t *bar, const Gri
 // stay in flight without a per-thread load chain in front of the stencil.
 // Arithmetic identical to k_sur_substep.  A copy wait that runs out sets bit 1
 // of *serr; the CTA waits (bounded) for its copies still in flight and leaves
-// its remaining tiles unstepped.
+// its remaining tiles unstepped.  gd.sub_skip_copy / gd.sub_wait_limit drive
+// that path in a test: the first tile's copies are left out and the wait
+// bound shortened, so the wait runs out on a phase nothing completes.
 template <int DIM, int MINB>
 __global__ void __launch_bounds__(kSubTile, MINB) k_sur_substep_tile(GridDev<float> gd, float dt, int cur)
 {
@@ -65,11 +67,14 @@ __global__ void __launch_bounds__(kSubTile, MINB) k_sur_substep_tile(GridDev<flo
     int64_t tile = blockIdx.x;
     if (tile >= ntiles) return;
     const bool det = gd.det != nullptr;
+    const uint32_t lim = gd.sub_wait_limit ? gd.sub_wait_limit : kSubWaitLimit;
     if (t == 0) {
         tc::mbar_init(&bar[0], 1);
         tc::mbar_init(&bar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        sub_issue(stg[0], &bar[0], gd, tile * kSubTile, det);
+        // (a failure-path test leaves the first tile's copies out: nothing
+        // completes that phase and its wait runs out)
+        if (!gd.sub_skip_copy) sub_issue(stg[0], &bar[0], gd, tile * kSubTile, det);
         if (tile + stride < ntiles) sub_issue(stg[1], &bar[1], gd, (tile + stride) * kSubTile, det);
     }
     __syncthreads();
@@ -78,11 +83,14 @@ __global__ void __launch_bounds__(kSubTile, MINB) k_sur_substep_tile(GridDev<flo
     float *__restrict__ Vn = gd.vg[cur ^ 1];
     for (uint32_t it = 0; tile < ntiles; tile += stride, ++it) {
         const int s = it & 1;
-        const bool ok = tc::mbar_wait(&bar[s], (it >> 1) & 1, kSubWaitLimit);
+        const bool ok = tc::mbar_wait(&bar[s], (it >> 1) & 1, lim);
         if (!__syncthreads_and(ok ? 1 : 0)) {
             if (t == 0) {
                 atomicOr(gd.serr, 2);
-                tc::mbar_wait(&bar[s], (it >> 1) & 1, kSubWaitLimit);
+                // let this CTA's copies in flight land before it leaves
+                // (the full bound: these are real copies; a first tile left
+                // out by the failure-path test has none)
+                if (it > 0 || !gd.sub_skip_copy) tc::mbar_wait(&bar[s], (it >> 1) & 1, kSubWaitLimit);
                 if (tile + stride < ntiles) tc::mbar_wait(&bar[s ^ 1], ((it + 1) >> 1) & 1, kSubWaitLimit);
             }
             return;

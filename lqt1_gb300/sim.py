@@ -195,6 +195,14 @@ class Sim:
                 "lqt_sim_surrogate_stats")
         return dict(macro_steps=m.value, offered=o.value, accepted=a.value, wait_timeouts=t.value)
 
+    def set_wait_test(self, skip_first_copy: bool, wait_limit: int = 0):
+        """Failure-path test (lqt_sim_set_wait_test): make the staged substep's
+        first tile wait of every CTA run out after wait_limit polls."""
+        L = N.lib()
+        L.lqt_sim_set_wait_test.argtypes = [C.c_void_p, C.c_int32, C.c_uint32]
+        N.check(L.lqt_sim_set_wait_test(self._h, int(bool(skip_first_copy)), int(wait_limit)),
+                "lqt_sim_set_wait_test")
+
     def surrogate_rejections(self):
         """Offered voxels that failed each residual check since the last
         reset: network bound, gate range, concentration, ionic V step."""

@@ -288,3 +288,35 @@ def test_macro_length_and_rejection_counters(lq, orc, net):
     np.testing.assert_array_equal(sim.get_state(), plain.get_state())   # every voxel ran the plain step
     sim.close()
     plain.close()
+
+
+def test_substep_wait_timeout_is_reported_and_recoverable(lq, net):
+    """Failure path of the staged substep's bounded waits, without a GPU
+    fault: a test setting leaves the first tile's copies of every CTA out, so
+    nothing completes that mbarrier phase and the wait runs out after a short
+    bound.  The kernel sets the error bit and returns; surrogate_stats reports
+    it, lqt_sim_check raises, and with the setting cleared the same
+    simulation steps on normally."""
+    v = lq.geometry.ventricle(nx=44, ny=44, nz=50, dx=0.2, a_out=4.0, c_out=8.0, wall=2.0, z_base=9.0,
+                              island_radius=1.5, stim_radius=1.2)
+    m = lq.model("baseline", gks_scale=0.5, pca_scale=2.0, gks_iso_scale=1.5)
+    sim = lq.Sim(v.types, 0.2, fibre=v.fibre, precision=lq.MIXED, model=m)
+    sim.set_protocol(bcl=800.0, s1_mask=v.s1_mask, s1_start=0.0, s1_duration=2.0, s1_strength=-52.0)
+    sim.set_surrogate(net)
+    sim.tune(4)
+    assert sim.substep_variant(105) == 105
+    sim.step(2 * net.nsub)
+    assert sim.surrogate_stats()["wait_timeouts"] == 0 and sim.check() == 0
+    sim.set_wait_test(True, 256)
+    sim.step(5)
+    assert sim.surrogate_stats()["wait_timeouts"] & 2
+    with pytest.raises(lq.LqtError):
+        sim.check()
+    sim.set_wait_test(False, 0)
+    sim.surrogate_stats(reset=True)
+    sim.step(100)
+    st = sim.surrogate_stats()
+    assert st["wait_timeouts"] == 0 and st["accepted"] > 0
+    assert sim.check() == 0
+    assert np.isfinite(sim.get_state()).all()
+    sim.close()
