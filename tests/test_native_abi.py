@@ -51,6 +51,33 @@ def test_invalid_arguments_are_rejected_without_a_gpu(lq):
     assert rc == 1
 
 
+def test_surrogate_arguments_are_rejected_without_a_gpu(lq):
+    """Training-pair ranges with a macro length that does not divide the
+    50-step graph span, or a non-zero reserved field, are refused before any
+    device work; so are NULL handles of the surrogate and tuning calls."""
+    from lqt1_gb300 import surrogate as S
+    L = S._bind_sur()
+
+    def ranges(nsub, reserved=0, prob=0.01):
+        return S.SurRanges((C.c_double * 2)(0.05, 1.0), (C.c_double * 2)(1.0, 2.2), (C.c_double * 2)(1.0, 2.0),
+                           (C.c_double * 2)(400.0, 2000.0), 0, 2, 0.02, 2.0, prob, 0.3, nsub, reserved)
+    n = C.c_int64()
+    for bad in (ranges(7), ranges(51), ranges(-5), ranges(10, reserved=1), ranges(10, prob=0.0)):
+        rc = L.lqt_sur_datagen(16, 1, C.byref(bad), C.c_void_p(16), C.c_void_p(16), 100, C.byref(n), None)
+        assert rc == lq._native.ERR_INVALID, lq.lib().lqt_last_error()
+    rc = L.lqt_sur_datagen(16, 1, None, C.c_void_p(16), C.c_void_p(16), 100, C.byref(n), None)
+    assert rc == lq._native.ERR_INVALID
+    lib = lq.lib()
+    lib.lqt_sim_substep_variant.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]
+    lib.lqt_sim_set_wait_test.argtypes = [C.c_void_p, C.c_int32, C.c_uint32]
+    lib.lqt_sim_surrogate_rejections.argtypes = [C.c_void_p, C.c_void_p]
+    assert lib.lqt_sim_substep_variant(None, 105, None, None) == lq._native.ERR_INVALID
+    assert lib.lqt_sim_set_wait_test(None, 1, 16) == lq._native.ERR_INVALID
+    assert lib.lqt_sim_surrogate_rejections(None, None) == lq._native.ERR_INVALID
+    assert lib.lqt_sim_step_async(None, 1) == lq._native.ERR_INVALID
+    assert lib.lqt_sim_sync(None) == lq._native.ERR_INVALID
+
+
 def _compare_maps(lq, orc, grid):
     from lqt1_gb300 import geometry as G
     tof, dst, src = G.mirror_map(grid)
