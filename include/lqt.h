@@ -373,14 +373,25 @@ int lqt_sim_boundary(const lqt_sim *s, int64_t *dst_host, int64_t *src_host,
  * that owns all device memory and hands out fixed buffers, or a stepping loop
  * that must not take the device-wide synchronisation of cudaMalloc/cudaFree.
  * Same sum as lqt_sim_set_electrodes / lqt_sim_get_ecg.  v_grid_dev: FP32 V of
- * the nx*ny*nz grid with mirror ghosts filled (1D: the strand itself);
- * tissue_index_dev: int32 grid index of each tissue voxel (NULL for 1D);
- * electrodes_host: nel*3 mm; phi_dev: nel doubles written on `stream`.
+ * the nx*ny*nz grid, x-major: voxel (x, y, z) at index (x*ny + y)*nz + z, with
+ * the empty voxels next to tissue holding their mirror source's V (1D: the
+ * strand itself, ny = nz = 1); tissue_index_dev: int32 grid index of each
+ * tissue voxel (NULL for 1D); positions are in the grid frame with voxel
+ * (x, y, z) at (x*dx, y*dx, z*dx) mm (origin at voxel 0, no offset);
+ * electrodes_host: nel*3 mm in that frame; phi_dev: nel doubles written on
+ * `stream`.  Precondition (2D/3D): no tissue voxel on a grid face, i.e.
+ * 1 <= x <= nx-2, 1 <= y <= ny-2 and, in 3D, 1 <= z <= nz-2.  The kernel
+ * checks every index before it reads V: a voxel that breaks this is skipped
+ * and every phi becomes NaN (the call is asynchronous, so this is how a bad
+ * index is reported; nothing outside the grid is read).
  * Limits: 1 <= nel <= 8; ntissue and the grid below 2^31.  Its scratch is a
- * fixed 128 KiB device array inside the library (every GPU that loads the
- * library holds it until exit); the first call on a device looks up that
- * array's address, so make it before any stream capture.  Calls that overlap
- * on the GPU share the array and race: serialise them. */
+ * fixed device array inside the library, 128 KiB of partials plus a 256-byte
+ * status word (every GPU that loads the library holds it until exit); the
+ * first call on a device looks up that array's address, so make it before any
+ * stream capture.  The address is cached per device for the process; after a
+ * cudaDeviceReset the first call's launch fails with LQT_ERR_CUDA and drops
+ * the cached address, and the next call looks it up again.  Calls that
+ * overlap on the GPU share the array and race: serialise them. */
 int lqt_ecg_grid_noalloc(const float *v_grid_dev, int32_t nx, int32_t ny,
                          int32_t nz, double dx, const int32_t *tissue_index_dev,
                          int64_t ntissue, const double *electrodes_host,

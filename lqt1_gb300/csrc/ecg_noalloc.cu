@@ -9,12 +9,19 @@
 // path needs (one FP64 partial per block and electrode) lives in a fixed
 // file-scope device array instead of a cudaMalloc'd buffer.
 //
-// The array is kNoAllocBlocks x kMaxEl doubles = 2048 x 8 x 8 B = 128 KiB.  It
-// is part of the library image, so every GPU that loads the library holds it
-// until the process exits.  All calls share it and it keeps the last call's
-// contents: each call overwrites exactly the partials it reads back, and calls
-// whose kernels overlap on the GPU (different streams, other threads) race on
-// it, so callers must serialise them.
+// The array is kNoAllocBlocks x kMaxEl doubles = 2048 x 8 x 8 B = 128 KiB of
+// partials plus a 256-byte tail that holds the call's status word.  It is part
+// of the library image, so every GPU that loads the library holds it until the
+// process exits.  All calls share it and it keeps the last call's contents:
+// each call clears the status word, overwrites exactly the partials it reads
+// back, and calls whose kernels overlap on the GPU (different streams, other
+// threads) race on it, so callers must serialise them.
+//
+// The caller's tissue index is checked on the device before any V access: a
+// voxel outside the grid or on a grid face (whose stencil would leave the grid
+// or wrap into the next row) is skipped and sets the status word, and the call
+// then writes NaN to every electrode.  The call stays asynchronous, so this is
+// how a bad index shows up: NaN in phi, never a read outside the V grid.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -32,17 +39,22 @@ constexpr int kNoAllocThreads = 256;
 constexpr int kMaxEl = 8;              // electrodes per call
 constexpr int kMaxDevices = 64;
 
-static __device__ __align__(256) double g_ecg_scratch[kNoAllocBlocks * kMaxEl];
+constexpr int kStatusSlot = kNoAllocBlocks * kMaxEl;   // first double of the 256-byte tail
+static __device__ __align__(256) double g_ecg_scratch[kNoAllocBlocks * kMaxEl + 32];
 
 struct Electrodes {
     float x[kMaxEl], y[kMaxEl], z[kMaxEl];
 };
 
 // Same sum as k_ecg_partial (3D form of PlotScript/plot1DECG_compare.py:89-105),
-// over a grid-stride loop so the number of partials is bounded.
+// over a grid-stride loop so the number of partials is bounded.  Grid index
+// g = (x*ny + y)*nz + z; a 2D/3D tissue voxel must have 1 <= x <= nx-2,
+// 1 <= y <= ny-2 and, in 3D, 1 <= z <= nz-2 (its stencil stays inside the
+// grid); any other index is skipped and flagged in *status.
 __global__ void __launch_bounds__(kNoAllocThreads)
-    k_ecg_noalloc_partial(const float *__restrict__ V, const int32_t *__restrict__ gidx, int64_t n, int64_t sx,
-                          int64_t sy, int dim, double dx, Electrodes el, int nel, double *__restrict__ partial)
+    k_ecg_noalloc_partial(const float *__restrict__ V, const int32_t *__restrict__ gidx, int64_t n, int64_t nx,
+                          int64_t ny, int64_t nz, int dim, double dx, Electrodes el, int nel,
+                          double *__restrict__ partial, unsigned int *__restrict__ status)
 {
     __shared__ double red[kNoAllocThreads / 32][kMaxEl];
     double acc[kMaxEl];
@@ -55,8 +67,15 @@ __global__ void __launch_bounds__(kNoAllocThreads)
             if (n > 1) h[0] = k == 0 ? V[1] - V[0] : (k == n - 1 ? V[k] - V[k - 1] : 0.5f * (V[k + 1] - V[k - 1]));
         } else {
             const int64_t g = gidx[k];
+            const int64_t sx = ny * nz, sy = dim == 2 ? 1 : nz;
             const int64_t x = g / sx, rem = g - x * sx;
             const int64_t y = rem / sy, z = rem - y * sy;
+            const bool inside = g >= 0 && x >= 1 && x <= nx - 2 && y >= 1 && y <= ny - 2 &&
+                                (dim == 2 || (z >= 1 && z <= nz - 2));
+            if (!inside) {
+                atomicOr(status, 1u);
+                continue;
+            }
             p[0] = (float)(x * dx);
             p[1] = (float)(y * dx);
             p[2] = (float)((dim == 3 ? z : 0) * dx);
@@ -88,11 +107,17 @@ __global__ void __launch_bounds__(kNoAllocThreads)
     }
 }
 
-// Sum the partials of the blocks that ran, in block order (deterministic).
+// Sum the partials of the blocks that ran, in block order (deterministic);
+// NaN for every electrode when the partial kernel flagged a bad voxel.
 __global__ void __launch_bounds__(kNoAllocThreads)
-    k_ecg_noalloc_final(const double *__restrict__ partial, int nblocks, int nel, double *__restrict__ out)
+    k_ecg_noalloc_final(const double *__restrict__ partial, int nblocks, int nel, const unsigned int *status,
+                        double *__restrict__ out)
 {
     __shared__ double red[kNoAllocThreads];
+    if (*status != 0u) {
+        if ((int)threadIdx.x < nel) out[threadIdx.x] = __longlong_as_double(0x7ff8000000000000LL);
+        return;
+    }
     for (int e = 0; e < nel; ++e) {
         double s = 0.0;
         for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += partial[b * kMaxEl + e];
@@ -130,6 +155,17 @@ int scratch_for_current_device(double **out)
     return LQT_OK;
 }
 
+// The cached address belongs to the device's context: drop it when a launch
+// fails, so a context torn down and re-created (cudaDeviceReset) gets a fresh
+// lookup on the next call.
+void forget_scratch_for_current_device()
+{
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return;
+    std::lock_guard<std::mutex> lock(g_setup_mu);
+    g_scratch_addr[dev] = nullptr;
+}
+
 }  // namespace
 
 extern "C" int lqt_ecg_grid_noalloc(const float *v_grid_dev, int32_t nx, int32_t ny, int32_t nz, double dx,
@@ -159,14 +195,21 @@ extern "C" int lqt_ecg_grid_noalloc(const float *v_grid_dev, int32_t nx, int32_t
     int64_t nb = (ntissue + kNoAllocThreads - 1) / kNoAllocThreads;
     if (nb > kNoAllocBlocks) nb = kNoAllocBlocks;
     cudaStream_t st = (cudaStream_t)stream;
-    k_ecg_noalloc_partial<<<(unsigned)nb, kNoAllocThreads, 0, st>>>(v_grid_dev, tissue_index_dev, ntissue,
-                                                                     (int64_t)ny * nz, dim == 2 ? 1 : nz, dim,
-                                                                     dx, el, nel, scratch);
-    cudaError_t e = cudaGetLastError();
+    unsigned int *status = reinterpret_cast<unsigned int *>(scratch + kStatusSlot);
+    // the status word keeps the last call's value: clear it first
+    cudaError_t e = cudaMemsetAsync(status, 0, sizeof(unsigned int), st);
     if (e == cudaSuccess) {
-        k_ecg_noalloc_final<<<1, kNoAllocThreads, 0, st>>>(scratch, (int)nb, nel, phi_dev);
+        k_ecg_noalloc_partial<<<(unsigned)nb, kNoAllocThreads, 0, st>>>(v_grid_dev, tissue_index_dev, ntissue, nx,
+                                                                         ny, nz, dim, dx, el, nel, scratch, status);
         e = cudaGetLastError();
     }
-    if (e != cudaSuccess) return lqt::fail(LQT_ERR_CUDA, std::string("lqt_ecg_grid_noalloc: ") + cudaGetErrorString(e));
+    if (e == cudaSuccess) {
+        k_ecg_noalloc_final<<<1, kNoAllocThreads, 0, st>>>(scratch, (int)nb, nel, status, phi_dev);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) {
+        forget_scratch_for_current_device();   // looked up again on the next call (e.g. after a device reset)
+        return lqt::fail(LQT_ERR_CUDA, std::string("lqt_ecg_grid_noalloc: ") + cudaGetErrorString(e));
+    }
     return LQT_OK;
 }

@@ -16,9 +16,10 @@
 #   libtpord_ref_{default,baseline,lqt1,lqt1half,suprep}.so
 #                                          TPORd.cc + oracle/ref_harness.inc
 #
-# Usage: oracle/build_ref.sh [REFERENCE_DIR]
+# Usage: oracle/build_ref.sh REFERENCE_DIR   (or LQT_REFERENCE=REFERENCE_DIR)
 set -euo pipefail
-REF=${1:-${LQT_REFERENCE:-/root/reference}}
+REF=${1:-${LQT_REFERENCE:-}}
+[ -n "$REF" ] || { echo "usage: $0 REFERENCE_DIR (a checkout of ShugangZhang/LQT1)" >&2; exit 2; }
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 [ -f "$REF/SingleCell/TPORd.cc" ] || { echo "reference not found at $REF" >&2; exit 2; }

@@ -1,7 +1,7 @@
 """Accuracy evaluations of the mixed form against the FP64 forms on the GPU and
 the CPU oracle, on the 2D sheet workload.
 
-  python -m lqt1_gb300.evaluate sheet2d [--n 600] [--t-end 2000] [--seed 7]
+  python tests/eval_sheet2d.py sheet2d [--n 600] [--t-end 2000] [--seed 7]
 
 2D sheet: n x n tissue at 0.15 mm, isotropic D = 0.154, bands 30/35/35 %
 endo/M/epi; one S1 plane wave from the x = 0 edge at t = 0 (2 ms x -52); S2 on
@@ -21,7 +21,8 @@ import time
 
 import numpy as np
 
-import lqt1_gb300 as lq
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+import lqt1_gb300 as lq  # noqa: E402
 
 
 def run_sheet(n, t_end, ci, precision, model, t_mid):

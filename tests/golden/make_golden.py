@@ -11,7 +11,7 @@ TPORd::update() through oracle/ref_harness.inc, and writes compact fixtures:
   ref_oned_cfg1.npz        OneD.cc with LQT1 GKs x0.5, ISO1 off, 2 ms stimulus
                            (the 1D strand workload), V samples, CV, pseudo-ECG
 
-Usage: python tests/golden/make_golden.py [REFERENCE_DIR]
+Usage: python tests/golden/make_golden.py REFERENCE_DIR
 """
 from __future__ import annotations
 
@@ -29,7 +29,9 @@ sys.path.insert(0, ROOT)
 from oracle import orc  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LQT_REFERENCE", "/root/reference")
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LQT_REFERENCE")
+if not REF:
+    sys.exit("usage: make_golden.py REFERENCE_DIR (a checkout of ShugangZhang/LQT1), or set LQT_REFERENCE")
 BIN = os.path.join(ROOT, "oracle", "_ref")
 
 
