@@ -23,6 +23,7 @@
 
 #include <stddef.h>
 #include <stdint.h>
+#include <stdio.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -103,8 +104,8 @@ int lqt_initial_state(double v0, double *state40_host);
 /* ======================================================================== *
  *  Batched cells: N independent TPORd instances on the device.
  *  Replaces `new TPORd(ct)`, `setDt`, `setIstim`, `setDVgap_dt`, `update()`,
- *  `getV`, `outputAllStates/readinAllStates` (SingleCell/TPORd.cc:137-376)
- *  for N cells at once.
+ *  `getV`, `getDvdt`, the current getters and `outputAllStates/readinAllStates`
+ *  (SingleCell/TPORd.cc:137-376) for N cells at once.
  * ======================================================================== */
 typedef struct lqt_cells lqt_cells;
 
@@ -130,6 +131,25 @@ int lqt_cells_update(lqt_cells *c, int64_t nsteps);
 /* Membrane potential and dV/dt of the last update (getV, getDvdt). */
 int lqt_cells_get_v(lqt_cells *c, double *v_host);
 int lqt_cells_get_dvdt(lqt_cells *c, double *dvdt_host);
+
+/* Currents of the last update, currents_host[n][6]: INa, ICaL, IKr, IKs, IK1
+ * (pA/pF) and |dV/dt| (mV/ms) -- getINa, getICaL, getIKr, getIKs, getIK1,
+ * getAbsDvdt (SingleCell/TPORd.cc:358-376).  Zero before the first update. */
+int lqt_cells_get_currents(lqt_cells *c, double *currents_host);
+
+/* Text state dump and restore of cells [first, first + count), cell after
+ * cell on an open stream: outputAllStates writes each cell's 40 states as
+ * "%4.10f\n" lines in the LQT_S_* order (SingleCell/TPORd.cc:200-252);
+ * readinAllStates reads 40 "%lf" values per cell in the same order
+ * (SingleCell/TPORd.cc:254-353).  The stream stays open and positioned after
+ * the cells, so several calls (or other writes) can share one file, as the
+ * reference's FILE* interface allows.  A read that runs out of values or finds
+ * a non-number returns LQT_ERR_IO and leaves every cell's state unchanged. */
+int lqt_cells_output_states(lqt_cells *c, int64_t first, int64_t count, FILE *f);
+int lqt_cells_readin_states(lqt_cells *c, int64_t first, int64_t count, FILE *f);
+/* The same text format for host state arrays (ncells x 40 doubles); no GPU. */
+int lqt_state_write_text(const double *state40, int64_t ncells, FILE *f);
+int lqt_state_read_text(double *state40, int64_t ncells, FILE *f);
 
 /* ======================================================================== *
  *  Batches of independent instances: single cells and 1D strands, run to

@@ -95,6 +95,11 @@ def lib():
         "lqt_cells_update": ([P, I64], I),
         "lqt_cells_get_v": ([P, P], I),
         "lqt_cells_get_dvdt": ([P, P], I),
+        "lqt_cells_get_currents": ([P, P], I),
+        "lqt_cells_output_states": ([P, I64, I64, P], I),
+        "lqt_cells_readin_states": ([P, I64, I64, P], I),
+        "lqt_state_write_text": ([P, I64, P], I),
+        "lqt_state_read_text": ([P, I64, P], I),
         "lqt_batch_create": ([C.POINTER(BatchParams), I32, P, P, P, I32, P, C.POINTER(P)], I),
         "lqt_batch_destroy": ([P], None),
         "lqt_batch_num_cells": ([P], I64),
@@ -137,6 +142,35 @@ def lib():
             f.argtypes, f.restype = args, res
     _lib = L
     return L
+
+
+class CFile:
+    """A C stdio stream (FILE*) for the entry points that take one, opened
+    and closed through the C library the native code uses."""
+
+    _libc = None
+
+    def __init__(self, path: str, mode: str):
+        if CFile._libc is None:
+            libc = C.CDLL(None)
+            libc.fopen.argtypes = [C.c_char_p, C.c_char_p]
+            libc.fopen.restype = C.c_void_p
+            libc.fclose.argtypes = [C.c_void_p]
+            CFile._libc = libc
+        self.ptr = CFile._libc.fopen(os.fsencode(path), mode.encode())
+        if not self.ptr:
+            raise OSError(f"cannot open {path} ({mode})")
+
+    def close(self):
+        if self.ptr:
+            CFile._libc.fclose(self.ptr)
+            self.ptr = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def check(code: int, where: str):

@@ -87,21 +87,29 @@ class TPORdCells:
         s = np.ascontiguousarray(s, dtype=np.float64).reshape(self.n, N.NSTATE)
         N.check(N.lib().lqt_cells_set_state(self._h, _p(s)), "lqt_cells_set_state")
 
-    def output_all_states(self, path: str, i: int = 0):
-        """Text dump of cell i in the reference's format (%4.10f per line)."""
-        s = self.get_state()[i]
-        with open(path, "w") as f:
-            for x in s:
-                f.write("%4.10f\n" % x)
+    def get_currents(self):
+        """[n, 6] INa, ICaL, IKr, IKs, IK1 (pA/pF) and |dV/dt| (mV/ms) of the
+        last update (TPORd getters, SingleCell/TPORd.cc:358-376)."""
+        out = np.zeros((self.n, 6))
+        N.check(N.lib().lqt_cells_get_currents(self._h, _p(out)), "lqt_cells_get_currents")
+        return out
 
-    def readin_all_states(self, path: str, i: int | None = None):
-        vals = np.loadtxt(path)
-        s = self.get_state()
-        if i is None:
-            s[:] = vals
-        else:
-            s[i] = vals
-        self.set_state(s)
+    def output_all_states(self, path: str, i: int = 0, count: int = 1):
+        """Text dump of cells [i, i + count) in the reference's format
+        (outputAllStates: 40 "%4.10f" lines per cell), through the C ABI."""
+        with N.CFile(path, "w") as f:
+            N.check(N.lib().lqt_cells_output_states(self._h, i, count, f.ptr), "lqt_cells_output_states")
+
+    def readin_all_states(self, path: str, i: int | None = None, count: int = 1):
+        """readinAllStates: 40 values per cell into cells [i, i + count); with
+        i = None, one cell's 40 values into every cell."""
+        with N.CFile(path, "r") as f:
+            if i is not None:
+                N.check(N.lib().lqt_cells_readin_states(self._h, i, count, f.ptr), "lqt_cells_readin_states")
+                return
+            one = np.zeros(N.NSTATE)
+            N.check(N.lib().lqt_state_read_text(_p(one), 1, f.ptr), "lqt_state_read_text")
+        self.set_state(np.repeat(one[None], self.n, 0))
 
 
 def initial_state(v0: float = -87.5) -> np.ndarray:

@@ -197,7 +197,7 @@ struct lqt_cells {
     cudaStream_t stream = nullptr;
     DevMem mem;
     uint8_t *ctype = nullptr;
-    double *ist = nullptr, *dvgap = nullptr, *dvdt = nullptr, *aos = nullptr;
+    double *ist = nullptr, *dvgap = nullptr, *dvdt = nullptr, *aos = nullptr, *cur = nullptr;
     void *v = nullptr, *gate = nullptr;
     double *conc = nullptr;
     ModelK *modelk = nullptr;
@@ -228,6 +228,7 @@ int lqt_cells_create(int64_t n, const uint8_t *types_host, int precision, const 
     const size_t rsz = precision == LQT_FP64 ? 8 : 4;
     rc = c->mem.alloc((void **)&c->ctype, n) | c->mem.alloc((void **)&c->ist, n * 8) |
          c->mem.alloc((void **)&c->dvgap, n * 8) | c->mem.alloc((void **)&c->dvdt, n * 8) |
+         c->mem.alloc((void **)&c->cur, n * 6 * 8) |
          c->mem.alloc((void **)&c->aos, n * 40 * 8) | c->mem.alloc(&c->v, c->ld * rsz) |
          c->mem.alloc(&c->gate, c->ld * rsz * kNGate) | c->mem.alloc((void **)&c->conc, c->ld * 8 * kNConc) |
          c->mem.alloc((void **)&c->modelk, sizeof(ModelK));
@@ -243,6 +244,7 @@ int lqt_cells_create(int64_t n, const uint8_t *types_host, int precision, const 
     if (e == cudaSuccess) e = cudaMemsetAsync(c->ist, 0, n * 8, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->dvgap, 0, n * 8, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->dvdt, 0, n * 8, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->cur, 0, n * 6 * 8, c->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(c->aos, init.data(), n * 320, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess)
         e = precision == LQT_FP64 ? launch_pack<double>(c->aos, c->soa<double>(), n, c->stream)
@@ -296,10 +298,10 @@ int lqt_cells_update(lqt_cells *c, int64_t nsteps)
     if (!c || nsteps < 0) return fail(LQT_ERR_INVALID, "lqt_cells_update: NULL handle or nsteps < 0");
     if (nsteps == 0) return LQT_OK;
     CK(c->precision == LQT_FP64
-           ? launch_cells_update<double>(c->soa<double>(), c->ctype, c->ist, c->dvgap, c->dvdt, c->modelk, nullptr,
-                                         c->stepk, c->n, nsteps, c->stream)
-           : launch_cells_update<float>(c->soa<float>(), c->ctype, c->ist, c->dvgap, c->dvdt, c->modelk, nullptr,
-                                        c->stepk, c->n, nsteps, c->stream));
+           ? launch_cells_update<double>(c->soa<double>(), c->ctype, c->ist, c->dvgap, c->dvdt, c->cur, c->modelk,
+                                         nullptr, c->stepk, c->n, nsteps, c->stream)
+           : launch_cells_update<float>(c->soa<float>(), c->ctype, c->ist, c->dvgap, c->dvdt, c->cur, c->modelk,
+                                        nullptr, c->stepk, c->n, nsteps, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return LQT_OK;
 }
@@ -320,6 +322,57 @@ int lqt_cells_get_dvdt(lqt_cells *c, double *dvdt_host)
     CK(cudaMemcpyAsync(dvdt_host, c->dvdt, c->n * 8, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return LQT_OK;
+}
+
+int lqt_cells_get_currents(lqt_cells *c, double *currents_host)
+{
+    if (!c || !currents_host) return fail(LQT_ERR_INVALID, "lqt_cells_get_currents: NULL");
+    CK(cudaMemcpyAsync(currents_host, c->cur, c->n * 6 * 8, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return LQT_OK;
+}
+
+// ---- text state I/O (TPORd::outputAllStates / readinAllStates) -------------
+int lqt_state_write_text(const double *state40, int64_t ncells, FILE *f)
+{
+    if (!state40 || !f || ncells < 0) return fail(LQT_ERR_INVALID, "lqt_state_write_text: NULL or ncells < 0");
+    for (int64_t i = 0; i < 40 * ncells; ++i)
+        if (fprintf(f, "%4.10f\n", state40[i]) < 0) return fail(LQT_ERR_IO, "lqt_state_write_text: write failed");
+    return LQT_OK;
+}
+
+int lqt_state_read_text(double *state40, int64_t ncells, FILE *f)
+{
+    if (!state40 || !f || ncells < 0) return fail(LQT_ERR_INVALID, "lqt_state_read_text: NULL or ncells < 0");
+    for (int64_t i = 0; i < 40 * ncells; ++i) {
+        double value;
+        if (fscanf(f, "%lf", &value) != 1)
+            return fail(LQT_ERR_IO, "lqt_state_read_text: value " + std::to_string(i) + " missing or not a number");
+        state40[i] = value;
+    }
+    return LQT_OK;
+}
+
+int lqt_cells_output_states(lqt_cells *c, int64_t first, int64_t count, FILE *f)
+{
+    if (!c || !f || first < 0 || count < 0 || first + count > c->n)
+        return fail(LQT_ERR_INVALID, "lqt_cells_output_states: NULL, or cells outside [0, n)");
+    std::vector<double> aos((size_t)c->n * 40);
+    int rc = lqt_cells_get_state(c, aos.data());
+    if (rc) return rc;
+    return lqt_state_write_text(aos.data() + 40 * first, count, f);
+}
+
+int lqt_cells_readin_states(lqt_cells *c, int64_t first, int64_t count, FILE *f)
+{
+    if (!c || !f || first < 0 || count < 0 || first + count > c->n)
+        return fail(LQT_ERR_INVALID, "lqt_cells_readin_states: NULL, or cells outside [0, n)");
+    std::vector<double> aos((size_t)c->n * 40);
+    int rc = lqt_cells_get_state(c, aos.data());
+    if (rc) return rc;
+    rc = lqt_state_read_text(aos.data() + 40 * first, count, f);
+    if (rc) return rc;
+    return lqt_cells_set_state(c, aos.data());
 }
 
 }  // extern "C"

@@ -23,11 +23,14 @@ namespace lqt {
 // ------------------------------------------------------------------------
 // Cell interface: n independent cells, nsteps updates with fixed inputs
 // (TPORd::setIstim / setDVgap_dt / update, SingleCell/TPORd.cc:358-379).
+// cur (or NULL): [n][6] INa, ICaL, IKr, IKs, IK1 and |dV/dt| of the last
+// update (getINa / getICaL / getIKr / getIKs / getIK1 / getAbsDvdt,
+// SingleCell/TPORd.cc:358-376).
 template <typename R>
 __global__ void __launch_bounds__(128) k_cells_update(SoA<R> s, const uint8_t *__restrict__ ctype,
                                                       const double *__restrict__ ist,
                                                       const double *__restrict__ dvgap, double *__restrict__ dvdt,
-                                                      const ModelK *__restrict__ models,
+                                                      double *__restrict__ cur, const ModelK *__restrict__ models,
                                                       const uint16_t *__restrict__ model_of, StepT<R> k, int64_t n,
                                                       int64_t nsteps)
 {
@@ -44,6 +47,15 @@ __global__ void __launch_bounds__(128) k_cells_update(SoA<R> s, const uint8_t *_
         store_cell(c, s, i);
         s.v[i] = c.v;
         if (dvdt) dvdt[i] = (double)o.dvdt;
+        if (cur) {
+            double *ci = cur + 6 * i;
+            ci[0] = (double)o.ina;
+            ci[1] = (double)o.ical;
+            ci[2] = (double)o.ikr;
+            ci[3] = (double)o.iks;
+            ci[4] = (double)o.ik1;
+            ci[5] = fabs((double)o.dvdt);
+        }
     }
 }
 
@@ -249,15 +261,15 @@ __global__ void __launch_bounds__(MAXT, MINB) k_batch(BatchDev<R> b, StepT<R> k)
 // ---- host-side launchers -------------------------------------------------
 template <typename R>
 cudaError_t launch_cells_update(const SoA<R> &s, const uint8_t *ctype, const double *ist, const double *dvgap,
-                                double *dvdt, const ModelK *models, const uint16_t *model_of, const StepK &k,
-                                int64_t n, int64_t nsteps, cudaStream_t stream)
+                                double *dvdt, double *cur, const ModelK *models, const uint16_t *model_of,
+                                const StepK &k, int64_t n, int64_t nsteps, cudaStream_t stream)
 {
     if (n <= 0) return cudaSuccess;
     const int bs = 128;
     int64_t nb = (n + bs - 1) / bs;
     if (nb > 152 * 64) nb = 152 * 64;
-    k_cells_update<R><<<(unsigned)nb, bs, 0, stream>>>(s, ctype, ist, dvgap, dvdt, models, model_of, step_as<R>(k), n,
-                                                       nsteps);
+    k_cells_update<R><<<(unsigned)nb, bs, 0, stream>>>(s, ctype, ist, dvgap, dvdt, cur, models, model_of,
+                                                       step_as<R>(k), n, nsteps);
     return cudaGetLastError();
 }
 
@@ -285,11 +297,11 @@ cudaError_t launch_batch(const BatchDev<R> &b, const StepK &k, int threads, int 
 }
 
 template cudaError_t launch_cells_update<double>(const SoA<double> &, const uint8_t *, const double *,
-                                                 const double *, double *, const ModelK *, const uint16_t *,
-                                                 const StepK &, int64_t, int64_t, cudaStream_t);
+                                                 const double *, double *, double *, const ModelK *,
+                                                 const uint16_t *, const StepK &, int64_t, int64_t, cudaStream_t);
 template cudaError_t launch_cells_update<float>(const SoA<float> &, const uint8_t *, const double *, const double *,
-                                                double *, const ModelK *, const uint16_t *, const StepK &, int64_t,
-                                                int64_t, cudaStream_t);
+                                                double *, double *, const ModelK *, const uint16_t *, const StepK &,
+                                                int64_t, int64_t, cudaStream_t);
 template cudaError_t launch_batch<double>(const BatchDev<double> &, const StepK &, int, int, int, cudaStream_t);
 template cudaError_t launch_batch<float>(const BatchDev<float> &, const StepK &, int, int, int, cudaStream_t);
 

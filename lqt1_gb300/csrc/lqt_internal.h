@@ -85,8 +85,8 @@ template <typename R> struct BatchDev {
 
 template <typename R>
 cudaError_t launch_cells_update(const SoA<R> &s, const uint8_t *ctype, const double *ist, const double *dvgap,
-                                double *dvdt, const ModelK *models, const uint16_t *model_of, const StepK &k,
-                                int64_t n, int64_t nsteps, cudaStream_t stream);
+                                double *dvdt, double *cur, const ModelK *models, const uint16_t *model_of,
+                                const StepK &k, int64_t n, int64_t nsteps, cudaStream_t stream);
 template <typename R>
 cudaError_t launch_batch(const BatchDev<R> &b, const StepK &k, int threads, int minb, int ctas, cudaStream_t stream);
 

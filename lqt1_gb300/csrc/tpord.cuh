@@ -128,6 +128,7 @@ template <typename R> struct CellState {
 template <typename R> struct StepOut {
     R dvdt;        // -(Iion + Ist) (TPORd.cc:928)
     R ical, iks;   // ICaL and IKs of the step (TPORd::getICaL / getIKs, SingleCell.cc:134-135)
+    R ina, ikr, ik1;   // INa, IKr, IK1 of the step (TPORd::getINa / getIKr / getIK1, TPORd.cc:365-370)
 };
 
 // One TPORd update.  ctype: 2 = EPI, 4 = MCELL, other = endocardial
@@ -451,6 +452,9 @@ __device__ __forceinline__ void tpord_step(CellState<R> &c, int ctype, const Mod
         out->dvdt = dV_dt;
         out->ical = ICaL;
         out->iks = IKs;
+        out->ina = INa;
+        out->ikr = IKr;
+        out->ik1 = IK1;
     }
 
     // CaMK and fluxes, TPORd.cc:939-995

@@ -486,6 +486,30 @@ void orc_cells_update(int64_t n, double *s, const uint8_t *ctype,
     }
 }
 
+/* nsteps updates of n cells, then the getters of the last update:
+ * cur[n][6] = getINa, getICaL, getIKr, getIKs, getIK1, getAbsDvdt
+ * (SingleCell/TPORd.cc:358-376; getAbsDvdt is abs(dV_dt) on a double,
+ * TPORd.cc:364). */
+void orc_cells_currents(int64_t n, double *s, const uint8_t *ctype,
+                        const lqt_model *m, double dt, const double *ist,
+                        const double *dvgap, int64_t nsteps, double *cur)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        double is = ist ? ist[i] : 0.0;
+        double dg = dvgap ? dvgap[i] : 0.0;
+        orc_aux a = {0};
+        for (int64_t k = 0; k < nsteps; ++k)
+            orc_update(s + i * LQT_NSTATE, ctype[i], m, dt, is, dg, &a);
+        double *c = cur + 6 * i;
+        c[0] = a.ina;
+        c[1] = a.ical;
+        c[2] = a.ikr;
+        c[3] = a.iks;
+        c[4] = a.ik1;
+        c[5] = fabs(a.dvdt);
+    }
+}
+
 /* OneD.cc:337-338 */
 int orc_in_window(double time, double bcl, double start, double dur)
 {

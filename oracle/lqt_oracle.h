@@ -42,6 +42,11 @@ void orc_update(double *s, int ctype, const lqt_model *m, double dt,
 void orc_cells_update(int64_t n, double *s, const uint8_t *ctype,
                       const lqt_model *m, double dt, const double *ist,
                       const double *dvgap, int64_t nsteps, int nthreads);
+/* The same updates, then the current getters of the last one, cur[n][6]:
+ * INa, ICaL, IKr, IKs, IK1, |dV/dt| (SingleCell/TPORd.cc:358-376). */
+void orc_cells_currents(int64_t n, double *s, const uint8_t *ctype,
+                        const lqt_model *m, double dt, const double *ist,
+                        const double *dvgap, int64_t nsteps, double *cur);
 
 /* SingleCell.cc:95-232: single cell paced at bcl for nbeats; APD statistics of
  * the last beat.  stats out: [rest, dvdt_max, overshoot, amplitude, apd20,

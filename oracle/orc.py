@@ -93,6 +93,7 @@ def lib():
         L.orc_initial_state.argtypes = [C.c_double, P]
         L.orc_update.argtypes = [P, C.c_int, C.POINTER(Model), C.c_double, C.c_double, C.c_double, P]
         L.orc_cells_update.argtypes = [C.c_int64, P, P, C.POINTER(Model), C.c_double, P, P, C.c_int64, C.c_int]
+        L.orc_cells_currents.argtypes = [C.c_int64, P, P, C.POINTER(Model), C.c_double, P, P, C.c_int64, P]
         L.orc_single_cell_run.argtypes = [C.c_int, C.POINTER(Model), C.c_double, C.c_double, C.c_double,
                                           C.c_double, C.c_double, C.c_double, C.c_double, P, C.c_int64, P,
                                           C.c_int64, P]
@@ -142,6 +143,19 @@ def cells_update(state, types, m: Model, dt=0.02, ist=None, dvgap=None, nsteps=1
     lib().orc_cells_update(state.shape[0], _p(state), _p(types), C.byref(m), dt, _p(ist), _p(dvgap),
                            nsteps, nthreads)
     return state
+
+
+def cells_currents(state, types, m: Model, dt=0.02, ist=None, dvgap=None, nsteps=1):
+    """In-place FP64 updates of n cells; returns [n, 6] INa, ICaL, IKr, IKs,
+    IK1, |dV/dt| of the last update (the TPORd getters)."""
+    assert state.dtype == np.float64 and state.flags.c_contiguous
+    types = np.ascontiguousarray(types, dtype=np.uint8)
+    ist = None if ist is None else np.ascontiguousarray(ist, dtype=np.float64)
+    dvgap = None if dvgap is None else np.ascontiguousarray(dvgap, dtype=np.float64)
+    cur = np.zeros((state.shape[0], 6))
+    lib().orc_cells_currents(state.shape[0], _p(state), _p(types), C.byref(m), dt, _p(ist), _p(dvgap), nsteps,
+                             _p(cur))
+    return cur
 
 
 def single_cell_run(ctype=MCELL, m: Model | None = None, v0=-87.5, dt=0.02, bcl=1000.0, nbeats=100.0,
@@ -275,6 +289,9 @@ def ref_lib(variant="default"):
         L.lqt_ref_strands.argtypes = [C.c_int64, C.c_int32, P, C.c_double, C.c_double, C.c_double, C.c_int64,
                                       C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]
         L.lqt_ref_strands.restype = C.c_int64
+        L.lqt_ref_currents.argtypes = [C.c_int64, P, P, C.c_double, P, P, C.c_int64, P]
+        L.lqt_ref_write_states.argtypes = [C.c_int64, P, C.c_char_p]
+        L.lqt_ref_read_states.argtypes = [C.c_int64, P, C.c_char_p]
         _ref_libs[variant] = L
     return _ref_libs[variant]
 
@@ -285,6 +302,30 @@ def ref_update(state, types, variant="default", dt=0.02, ist=None, dvgap=None, n
     dvgap = None if dvgap is None else np.ascontiguousarray(dvgap, dtype=np.float64)
     ref_lib(variant).lqt_ref_update(state.shape[0], _p(state), _p(types), dt, _p(ist), _p(dvgap), nsteps, None,
                                     nthreads)
+    return state
+
+
+def ref_currents(state, types, variant="default", dt=0.02, ist=None, dvgap=None, nsteps=1):
+    """The reference's updates and getters ([n, 6]: INa, ICaL, IKr, IKs, IK1, |dV/dt|)."""
+    types = np.ascontiguousarray(types, dtype=np.uint8)
+    ist = None if ist is None else np.ascontiguousarray(ist, dtype=np.float64)
+    dvgap = None if dvgap is None else np.ascontiguousarray(dvgap, dtype=np.float64)
+    cur = np.zeros((state.shape[0], 6))
+    ref_lib(variant).lqt_ref_currents(state.shape[0], _p(state), _p(types), dt, _p(ist), _p(dvgap), nsteps,
+                                      _p(cur))
+    return cur
+
+
+def ref_write_states(state, path, variant="default"):
+    """The reference's outputAllStates of each row of state, one file."""
+    state = np.ascontiguousarray(state, dtype=np.float64).reshape(-1, NSTATE)
+    assert ref_lib(variant).lqt_ref_write_states(state.shape[0], _p(state), path.encode()) == 0
+
+
+def ref_read_states(n, path, variant="default"):
+    """The reference's readinAllStates of n cells from one file."""
+    state = np.zeros((n, NSTATE))
+    assert ref_lib(variant).lqt_ref_read_states(n, _p(state), path.encode()) == 0
     return state
 
 

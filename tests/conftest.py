@@ -23,3 +23,10 @@ def orc():
 @pytest.fixture(scope="session")
 def golden_dir():
     return os.path.join(ROOT, "tests", "golden")
+
+
+@pytest.fixture(scope="session")
+def lq_lib():
+    """The native library (loads without a GPU; host-only entry points run)."""
+    import lqt1_gb300 as lq
+    return lq.lib()

@@ -10,6 +10,13 @@
 //        formats, mixed-form tissue run with a VTK frame every 500 steps
 //        (asynchronous writer) and V of every tissue voxel at the end in
 //        <outdir>/v_final.bin.
+//   drivers single <out.dat> <states.dat> <steps>    SingleCell.cc: one M cell
+//        through the Cell interface (setIstim, update, getV, getICaL, getIKs,
+//        getAbsDvdt), S1 -53 pA/pF x 1 ms at 50 ms of each 1000 ms cycle;
+//        rows "time V ICaL IKs" every step; the final state dumped with
+//        outputAllStates, read back with readinAllStates into a second cell
+//        and checked; prints the largest |dV/dt| seen.
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -137,12 +144,60 @@ static int tissue(const char *geom_path, const char *stim_path, int nx, int ny, 
     return 0;
 }
 
+static int single(const char *out, const char *states, long steps)
+{
+    // SingleCell.cc:45-51: BCL 1000, dt 0.02, -53 pA/pF x 1 ms at 50 ms
+    const double bcl = 1000.0, dt = 0.02, start = 50.0, dur = 1.0, strength = -53.0;
+    const uint8_t mcell = LQT_MCELL;
+    lqt_model m;
+    CHECK(lqt_model_preset(LQT_PRESET_CPU_DEFAULT, &m));
+    lqt_cells *c = nullptr;
+    CHECK(lqt_cells_create(1, &mcell, LQT_FP64, &m, dt, nullptr, &c));
+    FILE *f = std::fopen(out, "w");
+    if (!f) return 1;
+    double time = 0.0, dvdt_max = 0.0;
+    for (long step = 0; step < steps; ++step, time += dt) {
+        const double tb = time - std::floor(time / bcl) * bcl;
+        const double ist = (tb >= start && tb < start + dur) ? strength : 0.0;
+        CHECK(lqt_cells_set_inputs(c, &ist, nullptr));
+        CHECK(lqt_cells_update(c, 1));
+        double v, cur[6];
+        CHECK(lqt_cells_get_v(c, &v));
+        CHECK(lqt_cells_get_currents(c, cur));
+        if (cur[5] > dvdt_max) dvdt_max = cur[5];
+        std::fprintf(f, "%4.10f\t%4.10f\t%4.10f\t%4.10f\t\n", time, v, cur[1], cur[3]);
+    }
+    std::fclose(f);
+    // outputAllStates / readinAllStates round trip through a file
+    FILE *sf = std::fopen(states, "w");
+    if (!sf) return 1;
+    CHECK(lqt_cells_output_states(c, 0, 1, sf));
+    std::fclose(sf);
+    lqt_cells *c2 = nullptr;
+    CHECK(lqt_cells_create(1, &mcell, LQT_FP64, &m, dt, nullptr, &c2));
+    sf = std::fopen(states, "r");
+    if (!sf) return 1;
+    CHECK(lqt_cells_readin_states(c2, 0, 1, sf));
+    std::fclose(sf);
+    double a[LQT_NSTATE], b[LQT_NSTATE];
+    CHECK(lqt_cells_get_state(c, a));
+    CHECK(lqt_cells_get_state(c2, b));
+    double worst = 0.0;
+    for (int i = 0; i < LQT_NSTATE; ++i) worst = std::fmax(worst, std::fabs(a[i] - b[i]));
+    std::printf("dvdt_max %.6f readin_max_diff %.3g\n", dvdt_max, worst);
+    lqt_cells_destroy(c2);
+    lqt_cells_destroy(c);
+    return worst <= 5.1e-11 ? 0 : 3;
+}
+
 int main(int argc, char **argv)
 {
     if (argc >= 3 && !std::strcmp(argv[1], "oned")) return oned(argv[2]);
+    if (argc >= 5 && !std::strcmp(argv[1], "single")) return single(argv[2], argv[3], std::atol(argv[4]));
     if (argc >= 9 && !std::strcmp(argv[1], "tissue"))
         return tissue(argv[2], argv[3], std::atoi(argv[4]), std::atoi(argv[5]), std::atoi(argv[6]), std::atol(argv[7]),
                       argv[8]);
-    std::fprintf(stderr, "usage: drivers oned <out.dat> | tissue <geom> <stim> <nx> <ny> <nz> <steps> <outdir>\n");
+    std::fprintf(stderr, "usage: drivers oned <out.dat> | single <out.dat> <states.dat> <steps> | "
+                         "tissue <geom> <stim> <nx> <ny> <nz> <steps> <outdir>\n");
     return 2;
 }

@@ -75,3 +75,33 @@ def test_tissue_driver_reads_reference_files(drivers, tmp_path):
     assert (v_py > -30).any()                         # the stimulated wave is on its way
     frames = sorted(p for p in os.listdir(tmp_path) if p.startswith("ap_") and p.endswith(".vtk"))
     assert frames == ["ap_%d.vtk" % (k // 50) for k in range(0, steps, 500)]
+
+
+@pytest.mark.gpu
+def test_single_cell_driver_through_cell_interface(drivers, orc, tmp_path):
+    """SingleCell.cc's loop in C++ through lqt_cells_* (setIstim, update,
+    getV, getICaL, getIKs, getAbsDvdt, outputAllStates, readinAllStates):
+    one beat of an M cell against the FP64 oracle's update and getters."""
+    out, states = tmp_path / "single.dat", tmp_path / "states.dat"
+    steps = 20000
+    r = subprocess.run([drivers, "single", str(out), str(states), str(steps)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    rows = np.loadtxt(out)
+    assert rows.shape == (steps, 4)
+    # oracle: the same stimulus protocol, one update at a time
+    s = orc.initial_state(-87.5)
+    m = orc.model("default")
+    want = np.zeros((steps, 3))
+    dvdt_max = 0.0
+    for k in range(steps):
+        tb = rows[k, 0] - np.floor(rows[k, 0] / 1000.0) * 1000.0
+        ist = np.array([-53.0 if 50.0 <= tb < 51.0 else 0.0])
+        cur = orc.cells_currents(s, [orc.MCELL], m, ist=ist)[0]
+        want[k] = s[0, 0], cur[1], cur[3]
+        dvdt_max = max(dvdt_max, cur[5])
+    assert np.abs(rows[:, 1] - want[:, 0]).max() < 1e-3          # V, mV (printed to 1e-10)
+    scale = np.abs(want[:, 1:]).max(axis=0)
+    assert (np.abs(rows[:, 2:] - want[:, 1:]).max(axis=0) < 1e-4 * scale).all()
+    got_max = float(r.stdout.split()[1])
+    assert abs(got_max - dvdt_max) < 1e-6 * dvdt_max
+    assert len(open(states).read().split()) == 40

@@ -182,6 +182,70 @@ def test_accuracy_against_fp64(lq, torch, net):
         assert st["accepted"] >= 0.95 * st["offered"] > 0.5 * st["macro_steps"] * len(ref["apd90"])
 
 
+def test_network_beats_coarse_step_in_3d_tissue(lq, torch, net):
+    """What the trained network gains in tissue over the method without it:
+    a 100k-voxel ventricle shell of the 3D workload's construction and model
+    (IKs x0.5, ICaL x2, IKs-ISO x1.5), one beat (790 ms), against the FP64
+    form.  The same macro steps and window with the coarse TPORd step alone
+    (use_net = 0) have about twice the APD90 error and twice the V error
+    outside the upstroke; the network's errors are smaller on each, and both
+    forms stay inside the 1 ms / 0.1 ms / 0.5 mV bars.  Pseudo-ECG QT (six
+    electrodes, sampled every 0.1 ms) stays within 1 ms of FP64 for both."""
+    from lqt1_gb300.protocols import qt_from_ecg
+    v = lq.geometry.ventricle(nx=64, ny=64, nz=84, a_out=5.8, c_out=14.0, wall=3.0, z_base=15.5,
+                              island_radius=2.0, stim_radius=1.2)
+    m = lq.model("baseline", gks_scale=0.5, pca_scale=2.0, gks_iso_scale=1.5)
+    cx, cy, zm = v.spec.cx, v.spec.cy, v.spec.z_base - 0.5 * v.spec.c_out
+    ang = np.linspace(0, 2 * np.pi, 7)[:-1]
+    el = np.stack([cx + 25.8 * np.cos(ang), cy + 25.8 * np.sin(ang), np.full(6, zm)], 1)
+    nsteps, snap = 39500, 250
+
+    def run(prec, mode):
+        sim = lq.Sim(v.types, 0.2, fibre=v.fibre, precision=prec, model=m)
+        sim.set_protocol(bcl=800.0, s1_mask=v.s1_mask, s1_start=0.0, s1_duration=2.0, s1_strength=-52.0,
+                         s1_beats=1)
+        sim.set_electrodes(el, every=5)
+        if mode != "plain":
+            sim.set_surrogate(net, use_net=(mode == "net"))
+        snaps = []
+        for _ in range(nsteps // snap):
+            sim.step(snap)
+            snaps.append(sim.get_v())
+        out = dict(det=sim.detect(), snaps=np.array(snaps), ecg=sim.ecg(), bad=sim.check(),
+                   stats=sim.surrogate_stats() if mode != "plain" else None)
+        sim.close()
+        return out
+
+    ref = run(lq.FP64, "plain")
+    t_act = ref["det"]["t_act"]
+    ts = snap * 0.02 * np.arange(1, nsteps // snap + 1)
+    calm = ~((ts[:, None] >= t_act[None, :] - 1.0) & (ts[:, None] <= t_act[None, :] + 5.0))
+    # QT from the first sample (0.1 ms, before the wave leaves the apex)
+    qt_ref = [qt_from_ecg(ref["ecg"][1], ref["ecg"][0][:, j], 0.15, 800.0)[0] for j in range(6)]
+    assert np.isfinite(qt_ref).all()
+    err = {}
+    for mode in ("net", "coarse"):
+        d = run(lq.MIXED, mode)
+        assert d["bad"] == 0 and d["stats"]["wait_timeouts"] == 0
+        e = d["det"]["apd90"] - ref["det"]["apd90"]
+        both = (d["det"]["apd90"] > 0) & (ref["det"]["apd90"] > 0)
+        assert both.sum() == len(t_act)
+        dv = np.abs(d["snaps"] - ref["snaps"])[calm]
+        qt = [qt_from_ecg(d["ecg"][1], d["ecg"][0][:, j], 0.15, 800.0)[0] for j in range(6)]
+        err[mode] = dict(apd_max=float(np.abs(e).max()), apd_mean=float(np.abs(e).mean()),
+                         act_max=float(np.abs(d["det"]["t_act"] - t_act).max()), v_max=float(dv.max()),
+                         v_rms=float(np.sqrt((dv ** 2).mean())), qt_max=float(np.abs(np.subtract(qt, qt_ref)).max()),
+                         accepted=d["stats"]["accepted"] / (d["stats"]["macro_steps"] * len(t_act)))
+    n, c = err["net"], err["coarse"]
+    for e in (n, c):
+        assert e["act_max"] <= 0.1 + 1e-4 and e["apd_max"] <= 1.0 and e["v_max"] < 0.5 and e["qt_max"] <= 1.0, err
+        assert e["accepted"] > 0.9, err
+    assert n["apd_mean"] < 0.8 * c["apd_mean"], err
+    assert n["apd_max"] < c["apd_max"], err
+    assert n["v_rms"] < 0.8 * c["v_rms"], err
+    assert n["v_max"] < c["v_max"], err
+
+
 def test_speed_gain_over_plain_step(lq, torch, net):
     """3D ventricle shell (about 1M voxels), plateau and repolarisation: the
     surrogate form advances more cell-steps per second than the plain mixed
