@@ -95,6 +95,7 @@ static GemmArgs gemm(const __nv_bfloat16 *A, int64_t lda, int ta, const __nv_bfl
     GemmArgs g{};
     g.A = A;
     g.B = B;
+    g.err = nullptr;
     g.lda = lda;
     g.ldb = ldb;
     g.ta = ta;
@@ -108,6 +109,9 @@ static GemmArgs gemm(const __nv_bfloat16 *A, int64_t lda, int ta, const __nv_bfl
 // Forward + MSE gradient + backward into m->G (no update).
 static int forward_backward(lqt_mlp *m, const __nv_bfloat16 *X, const float *T, int64_t B)
 {
+    // every GEMM reports a tensor-core wait that ran out in m->err (checked
+    // where the host waits: lqt_mlp_gradients, lqt_mlp_train_step with a
+    // loss, lqt_mlp_get_params)
     if (B <= 0 || B % 16 != 0 || B > (int64_t)INT32_MAX) return fail(LQT_ERR_INVALID, "batch must be a positive multiple of 16");
     int rc = ensure_ws(m, B);
     if (rc) return rc;
@@ -116,31 +120,39 @@ static int forward_backward(lqt_mlp *m, const __nv_bfloat16 *X, const float *T, 
     const __nv_bfloat16 *W1 = m->Pb + kOW1, *W2 = m->Pb + kOW2, *W3 = m->Pb + kOW3;
     GemmArgs g = gemm(X, kMlpIn, 0, W1, kMlpIn, 1, b, kMlpHid, kMlpIn);
     g.epi = kEpiStore; g.bias = m->P + kOB1; g.C = m->Z1; g.Cb = m->H1; g.act = 1;
+    g.err = m->err;
     CK(launch_gemm_bf16(g, st));
     g = gemm(m->H1, kMlpHid, 0, W2, kMlpHid, 1, b, kMlpHid, kMlpHid);
     g.epi = kEpiStore; g.bias = m->P + kOB2; g.C = m->Z2; g.Cb = m->H2; g.act = 1;
+    g.err = m->err;
     CK(launch_gemm_bf16(g, st));
     g = gemm(m->H2, kMlpHid, 0, W3, kMlpHid, 1, b, kMlpOut, kMlpHid);
     g.epi = kEpiStore; g.bias = m->P + kOB3; g.C = m->Y;
+    g.err = m->err;
     CK(launch_gemm_bf16(g, st));
     CK(cudaMemsetAsync(m->loss, 0, 8, st));
     CK(launch_mse_grad(m->Y, T, B, m->nvalid, m->dY, m->loss, st));
     g = gemm(m->dY, kMlpOut, 0, W3, kMlpHid, 0, b, kMlpHid, kMlpOut);
     g.epi = kEpiDact; g.Z = m->Z2; g.Cb = m->dZ2;
+    g.err = m->err;
     CK(launch_gemm_bf16(g, st));
     g = gemm(m->dZ2, kMlpHid, 0, W2, kMlpHid, 0, b, kMlpHid, kMlpHid);
     g.epi = kEpiDact; g.Z = m->Z1; g.Cb = m->dZ1;
+    g.err = m->err;
     CK(launch_gemm_bf16(g, st));
     CK(cudaMemsetAsync(m->G, 0, kNParam * 4, st));
     const int ks = (int)std::min<int64_t>(128, std::max<int64_t>(1, B / 256));
     g = gemm(m->dY, kMlpOut, 1, m->H2, kMlpHid, 0, kMlpOut, kMlpHid, b);
     g.epi = kEpiAtomic; g.C = m->G + kOW3; g.ksplit = ks;
+    g.err = m->err;
     CK(launch_gemm_bf16(g, st));
     g = gemm(m->dZ2, kMlpHid, 1, m->H1, kMlpHid, 0, kMlpHid, kMlpHid, b);
     g.epi = kEpiAtomic; g.C = m->G + kOW2; g.ksplit = ks;
+    g.err = m->err;
     CK(launch_gemm_bf16(g, st));
     g = gemm(m->dZ1, kMlpHid, 1, X, kMlpIn, 0, kMlpHid, kMlpIn, b);
     g.epi = kEpiAtomic; g.C = m->G + kOW1; g.ksplit = ks;
+    g.err = m->err;
     CK(launch_gemm_bf16(g, st));
     CK(launch_colsum(m->dY, B, kMlpOut, m->G + kOB3, st));
     CK(launch_colsum(m->dZ2, B, kMlpHid, m->G + kOB2, st));
@@ -256,8 +268,11 @@ int lqt_mlp_gradients(lqt_mlp *m, const void *x_bf16_dev, const float *t_dev, in
     int rc = forward_backward(m, (const __nv_bfloat16 *)x_bf16_dev, t_dev, batch);
     if (rc) return rc;
     double l = 0;
+    int err = 0;
     CK(cudaMemcpyAsync(&l, m->loss, 8, cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaMemcpyAsync(&err, m->err, 4, cudaMemcpyDeviceToHost, m->stream));
     CK(cudaStreamSynchronize(m->stream));
+    if (err) return fail(LQT_ERR_TIMEOUT, "lqt_mlp_gradients: tensor-core completion wait timed out");
     if (loss) *loss = l / ((double)batch * m->nvalid);
     return LQT_OK;
 }
@@ -273,8 +288,11 @@ int lqt_mlp_train_step(lqt_mlp *m, const void *x_bf16_dev, const float *t_dev, i
     CK(launch_adam(m->P, m->G, m->M, m->V, m->Pb, kNParam, lr, b1, b2, 1e-8f, c1, c2, m->stream));
     if (loss) {
         double l = 0;
+        int err = 0;
         CK(cudaMemcpyAsync(&l, m->loss, 8, cudaMemcpyDeviceToHost, m->stream));
+        CK(cudaMemcpyAsync(&err, m->err, 4, cudaMemcpyDeviceToHost, m->stream));
         CK(cudaStreamSynchronize(m->stream));
+        if (err) return fail(LQT_ERR_TIMEOUT, "lqt_mlp_train_step: tensor-core completion wait timed out");
         *loss = l / ((double)batch * m->nvalid);
     }
     return LQT_OK;

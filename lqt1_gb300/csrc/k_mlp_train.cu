@@ -1,113 +1,160 @@
 // k_mlp_train.cu -- training kernels of the learned surrogate: a BF16
-// tensor-core GEMM (mma.sync m16n8k16, FP32 accumulate) with the epilogues the
-// forward and backward passes need, the loss gradient and the Adam update.
-// Training runs once, off the simulation's hot path; the per-macro-step
-// inference uses the tcgen05 kernel in k_mlp_tc.cu.
+// GEMM on the 5th-generation tensor cores (tcgen05.mma into a TMEM
+// accumulator, FP32) with the epilogues the forward and backward passes need,
+// the loss gradient and the Adam update.  Training runs once, off the
+// simulation's hot path; the per-macro-step inference uses the tcgen05 kernel
+// in k_sur_grid.cu / k_mlp_tc.cu.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "mlp.h"
+#include "tc.cuh"
 
 namespace lqt {
 
 namespace {
 
-constexpr int kBM = 64, kBN = 64, kBK = 16;
+constexpr int kTM = 128;                   // rows per CTA (TMEM lanes)
+constexpr int kKC = 64;                    // K per staged chunk (4 MMAs of K = 16)
+constexpr int kMaxN = 256;                 // N per CTA (one MMA)
+constexpr uint32_t kWaitLimit = 1u << 24;  // bounded mbarrier polls
+// dynamic shared memory per CTA: A chunk, B chunk, mbarrier and TMEM slot;
+// padded to 60 KB so that at most 3 CTAs share an SM (3 x 128 TMEM columns
+// of the SM's 512: tcgen05.alloc never has to wait)
+constexpr uint32_t kOffA = 0;
+constexpr uint32_t kOffB = kOffA + kTM * kKC * 2;
+constexpr uint32_t kOffBar = kOffB + kMaxN * kKC * 2;
+constexpr uint32_t kSmemBytes = 60 * 1024;
+static_assert(kOffBar + 16 <= kSmemBytes, "shared memory plan");
 
 __device__ __forceinline__ float sigm(float z) { return 1.0f / (1.0f + __expf(-z)); }
 
-__device__ __forceinline__ void mma16816(float *c, const uint32_t *a, const uint32_t *b)
+// One 8-element K chunk of row r of op(X) (X[r][k] = ta ? src[k * ld + r] :
+// src[r * ld + k]) for k = k0 .. k0 + 7, zero outside rows < R and k < kend.
+__device__ __forceinline__ uint4 load_chunk8(const __nv_bfloat16 *src, int64_t ld, int t, int r, int R, int k0,
+                                             int kend)
 {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+    if (r >= R) return make_uint4(0, 0, 0, 0);
+    if (!t && k0 + 8 <= kend && (ld & 7) == 0 && (k0 & 7) == 0)
+        return *reinterpret_cast<const uint4 *>(src + (int64_t)r * ld + k0);
+    uint32_t p[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        uint16_t h[2];
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int k = k0 + 2 * i + j;
+            __nv_bfloat16 v = __float2bfloat16(0.0f);
+            if (k < kend) v = t ? src[(int64_t)k * ld + r] : src[(int64_t)r * ld + k];
+            h[j] = __bfloat16_as_ushort(v);
+        }
+        p[i] = (uint32_t)h[0] | ((uint32_t)h[1] << 16);
+    }
+    return make_uint4(p[0], p[1], p[2], p[3]);
 }
 
-__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi)
+// C[M][N] (epilogue) = op(A)[M][K] * op(B)[K][N].  One CTA of 128 threads per
+// 128-row tile and (for the split weight gradients) K range: the tile's A rows
+// and all N rows of op(B)^T are staged chunk by chunk in the K-major core
+// layout; one elected thread issues the MMAs and commits to an mbarrier; the
+// accumulator (row m in TMEM lane m) goes through the epilogue by its thread.
+__global__ void __launch_bounds__(128) k_gemm_tc(GemmArgs g)
 {
-    __nv_bfloat162 v;
-    v.x = lo;
-    v.y = hi;
-    return *reinterpret_cast<uint32_t *>(&v);
-}
-
-// 128 threads, CTA tile 64 x 64, warp tile 32 x 32 (2 x 4 mma tiles).
-__global__ void __launch_bounds__(128) k_gemm_bf16(GemmArgs g)
-{
-    __shared__ __nv_bfloat16 sA[kBM][kBK + 8];
-    __shared__ __nv_bfloat16 sB[kBK][kBN + 8];
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int m0 = blockIdx.y * kBM, n0 = blockIdx.x * kBN;
-    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
-    const int grp = lane >> 2, tig = lane & 3;
-    float acc[2][4][4] = {};
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kOffBar);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + kOffBar + 8);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int m0 = blockIdx.y * kTM;
+    const int npad = (g.N + 15) / 16 * 16;
+    uint32_t ncols = 32;
+    while ((int)ncols < npad) ncols <<= 1;
     int kbeg = 0, kend = g.K;
     if (g.epi == kEpiAtomic && g.ksplit > 1) {
-        const int chunk = ((g.K + g.ksplit - 1) / g.ksplit + kBK - 1) / kBK * kBK;
+        const int chunk = ((g.K + g.ksplit - 1) / g.ksplit + kKC - 1) / kKC * kKC;
         kbeg = blockIdx.z * chunk;
         kend = min(g.K, kbeg + chunk);
     }
-    const __nv_bfloat16 zero = __float2bfloat16(0.0f);
-    for (int k0 = kbeg; k0 < kend; k0 += kBK) {
-        for (int i = tid; i < kBM * kBK; i += 128) {
-            const int r = i / kBK, c = i % kBK;
-            const int m = m0 + r, k = k0 + c;
-            __nv_bfloat16 v = zero;
-            if (m < g.M && k < kend) v = g.ta ? g.A[(int64_t)k * g.lda + m] : g.A[(int64_t)m * g.lda + k];
-            sA[r][c] = v;
+    if (tid == 0) {
+        tc::mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) tc::tmem_alloc(tslot, ncols);
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = *tslot;
+    const uint32_t idesc = tc::idesc_bf16_f32(kTM, npad);
+    uint32_t phase = 0;
+    bool ok = true;
+    int nchunk = 0;
+    for (int k0 = kbeg; k0 < kend && ok; k0 += kKC, ++nchunk) {
+        // stage: consecutive threads take consecutive rows (coalesced for the
+        // transposed operands, whose rows are contiguous in memory)
+        for (int c = tid; c < kTM * (kKC / 8); c += 128) {
+            const int r = c % kTM, kg = c / kTM;
+            *reinterpret_cast<uint4 *>(smem + kOffA + tc::kmaj_off(r, kg * 8, kKC)) =
+                load_chunk8(g.A, g.lda, g.ta, m0 + r, g.M, k0 + kg * 8, kend);
         }
-        for (int i = tid; i < kBK * kBN; i += 128) {
-            const int r = i / kBN, c = i % kBN;
-            const int k = k0 + r, n = n0 + c;
-            __nv_bfloat16 v = zero;
-            if (n < g.N && k < kend) v = g.tb ? g.B[(int64_t)n * g.ldb + k] : g.B[(int64_t)k * g.ldb + n];
-            sB[r][c] = v;
+        for (int c = tid; c < npad * (kKC / 8); c += 128) {
+            const int r = c % npad, kg = c / npad;
+            // op(B)^T row n: B[n][k] when stored transposed (tb), else B[k][n]
+            *reinterpret_cast<uint4 *>(smem + kOffB + tc::kmaj_off(r, kg * 8, kKC)) =
+                load_chunk8(g.B, g.ldb, !g.tb, r, g.N, k0 + kg * 8, kend);
         }
+        tc::fence_proxy_async();
+        tc::fence_before();
         __syncthreads();
-#pragma unroll
-        for (int mi = 0; mi < 2; ++mi) {
-            uint32_t a[4];
-            const int r = wm + mi * 16 + grp;
-            a[0] = pack2(sA[r][tig * 2], sA[r][tig * 2 + 1]);
-            a[1] = pack2(sA[r + 8][tig * 2], sA[r + 8][tig * 2 + 1]);
-            a[2] = pack2(sA[r][tig * 2 + 8], sA[r][tig * 2 + 9]);
-            a[3] = pack2(sA[r + 8][tig * 2 + 8], sA[r + 8][tig * 2 + 9]);
-#pragma unroll
-            for (int ni = 0; ni < 4; ++ni) {
-                uint32_t b[2];
-                const int c = wn + ni * 8 + grp;
-                b[0] = pack2(sB[tig * 2][c], sB[tig * 2 + 1][c]);
-                b[1] = pack2(sB[tig * 2 + 8][c], sB[tig * 2 + 9][c]);
-                mma16816(acc[mi][ni], a, b);
-            }
+        if (tid == 0) {
+            tc::fence_after();
+            const uint32_t lbo = 128, sbo = (kKC / 8) * 128;
+            const uint32_t a0 = tc::smem_u32(smem + kOffA), b0 = tc::smem_u32(smem + kOffB);
+            for (int kk = 0; kk < kKC / 16; ++kk)
+                tc::mma_bf16(tmem, tc::smem_desc(a0 + kk * 256, lbo, sbo), tc::smem_desc(b0 + kk * 256, lbo, sbo),
+                             idesc, (nchunk > 0 || kk > 0) ? 1u : 0u);
+            tc::mma_commit(bar);
         }
+        // the chunk's smem is reused only after its MMAs completed; the
+        // decision is made for the whole CTA at once
+        const bool w_ok = tc::mbar_wait(bar, phase, kWaitLimit);
+        if (!__syncthreads_and(w_ok ? 1 : 0)) {
+            if (!w_ok) tc::mbar_wait(bar, phase, kWaitLimit);   // let the MMAs in flight land before TMEM is freed
+            if (tid == 0 && g.err) atomicExch(g.err, 2);
+            ok = false;
+        }
+        phase ^= 1;
+        tc::fence_after();
         __syncthreads();
     }
+    if (ok && nchunk > 0) {
+        const int m = m0 + tid;
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int n0 = 0; n0 < g.N; n0 += 16) {
+            float v[16];
+            tc::tmem_ld16(taddr + n0, v);              // whole warp
+            if (m >= g.M) continue;
 #pragma unroll
-    for (int mi = 0; mi < 2; ++mi)
-#pragma unroll
-        for (int ni = 0; ni < 4; ++ni)
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const int m = m0 + wm + mi * 16 + grp + (e >= 2 ? 8 : 0);
-                const int n = n0 + wn + ni * 8 + tig * 2 + (e & 1);
-                if (m >= g.M || n >= g.N) continue;
+            for (int i = 0; i < 16; ++i) {
+                const int n = n0 + i;
+                if (n >= g.N) break;
                 const int64_t o = (int64_t)m * g.N + n;
-                float v = acc[mi][ni][e];
+                float x = v[i];
                 if (g.epi == kEpiStore) {
-                    if (g.bias) v += g.bias[n];
-                    if (g.C) g.C[o] = v;
-                    if (g.Cb) g.Cb[o] = __float2bfloat16(g.act ? v * sigm(v) : v);
+                    if (g.bias) x += g.bias[n];
+                    if (g.C) g.C[o] = x;
+                    if (g.Cb) g.Cb[o] = __float2bfloat16(g.act ? x * sigm(x) : x);
                 } else if (g.epi == kEpiDact) {
-                    const float z = g.Z[o], s = sigm(z);
-                    g.Cb[o] = __float2bfloat16(v * (s + z * s * (1.0f - s)));
+                    const float z = g.Z[o], sz = sigm(z);
+                    g.Cb[o] = __float2bfloat16(x * (sz + z * sz * (1.0f - sz)));
                 } else {
-                    atomicAdd(&g.C[o], v);
+                    atomicAdd(&g.C[o], x);
                 }
             }
+        }
+    }
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, ncols);
 }
 
 }  // namespace
@@ -115,8 +162,12 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(GemmArgs g)
 cudaError_t launch_gemm_bf16(const GemmArgs &g, cudaStream_t st)
 {
     if (g.M <= 0 || g.N <= 0 || g.K <= 0) return cudaSuccess;
-    dim3 grid((g.N + kBN - 1) / kBN, (g.M + kBM - 1) / kBM, g.epi == kEpiAtomic && g.ksplit > 1 ? g.ksplit : 1);
-    k_gemm_bf16<<<grid, 128, 0, st>>>(g);
+    if (g.N > kMaxN) return cudaErrorInvalidValue;
+    static std::atomic<uint64_t> attr_done{0};
+    cudaError_t e = tc::smem_attr_once(k_gemm_tc, kSmemBytes, attr_done);
+    if (e != cudaSuccess) return e;
+    dim3 grid(1, (g.M + kTM - 1) / kTM, g.epi == kEpiAtomic && g.ksplit > 1 ? g.ksplit : 1);
+    k_gemm_tc<<<grid, 128, kSmemBytes, st>>>(g);
     return cudaGetLastError();
 }
 

@@ -47,6 +47,7 @@ struct GemmArgs {
     int act;                     // kEpiStore: 1 = SiLU for Cb
     const float *Z;              // kEpiDact: pre-activation [M][N]
     int ksplit;                  // kEpiAtomic: split K over grid.z
+    int *err;                    // set to 2 if a tensor-core completion wait ran out (or NULL)
 };
 cudaError_t launch_gemm_bf16(const GemmArgs &g, cudaStream_t st);
 

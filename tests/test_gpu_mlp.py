@@ -1,6 +1,7 @@
 """GPU checks of the surrogate network's hand-written tensor-core kernels:
-tcgen05 inference and mma.sync training gradients against the FP64 CPU
-reference (oracle/mlp_ref.py), which is itself checked by finite differences."""
+tcgen05 inference and tcgen05 training GEMMs (forward, backward, split-K
+weight gradients) against the FP64 CPU reference (oracle/mlp_ref.py), which is
+itself checked by finite differences."""
 import numpy as np
 import pytest
 
@@ -47,13 +48,15 @@ def test_tcgen05_inference_matches_reference(torch_cuda):
 
 
 @pytest.mark.gpu
-def test_training_gradients_match_reference(torch_cuda):
+@pytest.mark.parametrize("B", [512, 8192 + 48])
+def test_training_gradients_match_reference(torch_cuda, B):
+    """Batch 512 (two K slices per weight gradient) and the training batch
+    plus a partial row tile (33 K slices of 256 rows; a 48-row tail)."""
     torch = torch_cuda
     from lqt1_gb300.surrogate import Mlp
     m = Mlp(seed=4)
     p = m.params()
     rng = np.random.default_rng(2)
-    B = 512
     x = rng.normal(0, 1, (B, 48)).astype(np.float32)
     t = rng.normal(0, 1, (B, 48)).astype(np.float32)
     loss = m.gradients(torch.from_numpy(x).cuda().to(torch.bfloat16), torch.from_numpy(t).cuda())
