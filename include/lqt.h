@@ -366,11 +366,15 @@ int lqt_sim_tune(lqt_sim *s, int32_t variant, int32_t *chosen, float *ms_per_var
  * persistent CTAs that stage each 256-voxel tile's streamed rows (rate, index,
  * tensor, control, detector flag) in shared memory with bulk asynchronous
  * copies, two tiles in flight, at 5, 6, 8 CTAs/SM (2D/3D anisotropic grids;
- * elsewhere the direct kernel runs).  variant >= 0 forces one (the autotuner
- * then keeps it); variant < 0 only reports the current one.  All variants give
- * bit-identical results.  ms_per_variant (or NULL): 6 mean milliseconds per
- * step from the last autotune, in the order 5, 6, 8, 105, 106, 108 (zeros if
- * it has not run). */
+ * elsewhere the direct kernel runs); 203, 204 = the same with each tile's
+ * V halo (the box of the dense V grid its 19-point stencils reach, copied as
+ * z-segments of its columns) staged in shared memory too, at 3, 4 CTAs/SM
+ * (3D anisotropic grids with nz a multiple of 4; elsewhere 105 runs).
+ * variant >= 0 forces one (the autotuner then keeps it); variant < 0 only
+ * reports the current one.  All variants give bit-identical results.
+ * ms_per_variant (or NULL): 8 mean milliseconds per step from the last
+ * autotune, in the order 5, 6, 8, 105, 106, 108, 203, 204 (zeros if it has not
+ * run). */
 int lqt_sim_substep_variant(lqt_sim *s, int32_t variant, int32_t *chosen, float *ms_per_variant);
 
 /* Instrumentation (no counterpart in the reference, which has no timing):
@@ -505,9 +509,11 @@ void lqt_vtk_writer_destroy(lqt_vtk_writer *w);
  *  48 -> 128 -> 128 -> 48 with SiLU, BF16 weights, FP32 accumulation.
  *  Parameters are one FP32 block of lqt_mlp_num_params() floats:
  *  W1 [128][48], b1 [128], W2 [128][128], b2 [128], W3 [48][128], b3 [48]
- *  (weights [out][in]).  Inference runs on the tcgen05 tensor cores with the
- *  accumulators in TMEM; training (forward, MSE gradient, backward, Adam)
- *  uses BF16 mma.sync tensor-core GEMMs.  Device buffers belong to the caller.
+ *  (weights [out][in]).  Inference and the training GEMMs (forward, backward
+ *  and weight gradients) run on the tcgen05 tensor cores with the
+ *  accumulators in TMEM; every tensor-core completion wait is bounded and a
+ *  wait that runs out makes the next call that waits return LQT_ERR_TIMEOUT.
+ *  Device buffers belong to the caller.
  * ======================================================================== */
 typedef struct lqt_mlp lqt_mlp;
 int lqt_mlp_create(uint64_t seed, void *stream, lqt_mlp **out);
@@ -660,6 +666,14 @@ int lqt_geom_ventricle(const lqt_ventricle_spec *spec, uint8_t *types,
 int lqt_geom_mirror_map(int32_t nx, int32_t ny, int32_t nz,
                         const uint8_t *types, int32_t *tissue_of,
                         int64_t *bnd_dst, int64_t *bnd_src, int64_t *nbnd);
+/* The same numbering and mirror-boundary map built on the GPU (one thread per
+ * grid voxel, then an ordered compaction), bit-identical to the host builder;
+ * lqt_sim_create uses it.  Host arrays in and out, as lqt_geom_mirror_map;
+ * stream: a cudaStream_t or NULL.  Grid below 2^31 voxels. */
+int lqt_geom_mirror_map_gpu(int32_t nx, int32_t ny, int32_t nz,
+                            const uint8_t *types, int32_t *tissue_of,
+                            int64_t *bnd_dst, int64_t *bnd_src, int64_t *nbnd,
+                            void *stream);
 
 #ifdef __cplusplus
 }

@@ -47,6 +47,7 @@ struct lqt_sim {
     void *vg[2] = {nullptr, nullptr};
     void *gate = nullptr, *d6 = nullptr, *b3 = nullptr, *coeff = nullptr, *dcoeff = nullptr;
     __half2 *d6h = nullptr, *b3h = nullptr;   // FP16 tensor copies for the surrogate substep (pad_tiles rows)
+    int32_t *vbox_hdr = nullptr, *vli = nullptr;   // V-halo boxes of the 3D substep (k_sur_substep_vbox)
     double *conc = nullptr, *aos = nullptr;
     int32_t *gidx = nullptr, *bnd_dst = nullptr, *bnd_src = nullptr;
     uint8_t *ctl = nullptr;
@@ -180,6 +181,8 @@ struct lqt_sim {
         g.serr = in_macro ? sur_err : nullptr;
         g.d6h = in_macro ? d6h : nullptr;
         g.b3h = in_macro ? b3h : nullptr;
+        g.vbox_hdr = in_macro ? vbox_hdr : nullptr;
+        g.vli = in_macro ? vli : nullptr;
         g.sub_skip_copy = sub_skip_copy;
         g.sub_wait_limit = sub_wait_limit;
         return g;
@@ -194,6 +197,45 @@ template <typename R> GridDev<R> devf(const lqt_sim *s)
     GridDev<R> g = s->dev<R>();
     g.diso = (R)s->diso;
     return g;
+}
+
+// V-halo boxes of the 3D substep, per tile of kSubTile tissue voxels (in
+// tissue order): the box spans the tile's columns one voxel beyond in x and y
+// and its z range one voxel beyond, z rounded out to multiples of 4 and kept
+// inside the column (nz is a multiple of 4; tissue is off the grid faces, so
+// the box stays inside the grid).  hdr: 8 ints per tile {ok, zlo, xlo, ylo,
+// bx, by, bz, 0}, ok = 0 when the box exceeds kVBoxFloats or kVBoxMaxCols
+// columns; li: each voxel's index in its tile's box (pad_tiles entries).
+void build_vboxes(const std::vector<int64_t> &cells, int64_t nx, int64_t ny, int64_t nz, std::vector<int32_t> &hdr,
+                  std::vector<int32_t> &li)
+{
+    const int64_t n = (int64_t)cells.size(), ntiles = (n + kSubTile - 1) / kSubTile;
+    hdr.assign(ntiles * 8, 0);
+    li.assign(pad_tiles(n), 0);
+    for (int64_t T = 0; T < ntiles; ++T) {
+        const int64_t k0 = T * kSubTile, k1 = std::min(n, k0 + kSubTile);
+        int64_t xmin = nx, xmax = -1, ymin = ny, ymax = -1, zmin = nz, zmax = -1;
+        for (int64_t k = k0; k < k1; ++k) {
+            const int64_t g = cells[k], x = g / (ny * nz), y = (g / nz) % ny, z = g % nz;
+            xmin = std::min(xmin, x); xmax = std::max(xmax, x);
+            ymin = std::min(ymin, y); ymax = std::max(ymax, y);
+            zmin = std::min(zmin, z); zmax = std::max(zmax, z);
+        }
+        const int64_t xlo = xmin - 1, ylo = ymin - 1, zlo = (zmin - 1) / 4 * 4;
+        const int64_t bx = xmax + 1 - xlo + 1, by = ymax + 1 - ylo + 1;
+        const int64_t bz = std::min(nz - zlo, (zmax + 1 - zlo + 1 + 3) / 4 * 4);
+        const bool ok = xlo >= 0 && ylo >= 0 && zmin >= 1 && xmax + 1 < nx && ymax + 1 < ny && zmax + 1 < nz &&
+                        bx * by <= kVBoxMaxCols && bx * by * bz <= kVBoxFloats;
+        int32_t *h = &hdr[T * 8];
+        h[0] = ok;
+        h[1] = (int32_t)zlo; h[2] = (int32_t)xlo; h[3] = (int32_t)ylo;
+        h[4] = (int32_t)bx; h[5] = (int32_t)by; h[6] = (int32_t)bz;
+        if (!ok) continue;
+        for (int64_t k = k0; k < k1; ++k) {
+            const int64_t g = cells[k], x = g / (ny * nz), y = (g / nz) % ny, z = g % nz;
+            li[k] = (int32_t)(((x - xlo) * by + (y - ylo)) * bz + (z - zlo));
+        }
+    }
 }
 
 // Recompute S1 windows for steps [0, horizon) and the S2 window; upload.
@@ -576,7 +618,12 @@ int lqt_sim_create(const lqt_sim_params *params, const lqt_geometry *geom, lqt_s
             s->tm.tissue_of[i] = i;
         }
     } else {
-        build_tissue_map(nx, ny, nz, geom->cell_type, s->tm);
+        // numbering and mirror-boundary map built on the GPU (k_geom.cu)
+        rc = build_tissue_map_gpu(nx, ny, nz, geom->cell_type, s->stream, s->tm);
+        if (rc) {
+            delete s;
+            return rc;
+        }
     }
     s->ntissue = (int64_t)s->tm.cells.size();
     s->nbnd = (int64_t)s->tm.bnd_dst.size();
@@ -1207,6 +1254,16 @@ int lqt_sim_set_surrogate(lqt_sim *s, lqt_mlp *m, const lqt_sur_config *cfg)
         CK(cudaMemsetAsync(s->d6h, 0, np * 12, s->stream));
         CK(cudaMemsetAsync(s->b3h, 0, np * 8, s->stream));
         CK(launch_tensor_f16((const float *)s->d6, (const float *)s->b3, s->ntissue, s->d6h, s->b3h, s->stream));
+    }
+    // the V-halo boxes of the 3D substep (whole z-segments: nz a multiple of 4)
+    if (s->d6 && s->dim == 3 && s->nz % 4 == 0 && !s->vbox_hdr) {
+        std::vector<int32_t> hdr, li;
+        build_vboxes(s->tm.cells, s->nx, s->ny, s->nz, hdr, li);
+        if (s->mem.alloc((void **)&s->vbox_hdr, hdr.size() * 4) | s->mem.alloc((void **)&s->vli, li.size() * 4))
+            return LQT_ERR_NOMEM;
+        CK(cudaMemcpyAsync(s->vbox_hdr, hdr.data(), hdr.size() * 4, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(s->vli, li.data(), li.size() * 4, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
     }
     // NaN everywhere (the tile padding included): plain steps until the first
     // macro-step boundary

@@ -15,6 +15,7 @@
 
 #include "../../include/lqt.h"
 #include "geometry.h"
+#include "mirror_tables.h"
 
 namespace lqt {
 
@@ -22,24 +23,14 @@ namespace {
 
 inline int64_t gi(int64_t ny, int64_t nz, int64_t x, int64_t y, int64_t z) { return (x * ny + y) * nz + z; }
 
-// Occupancy terms {slot, weight kind (1, 2 = 1/sqrt2, 3 = 1/sqrt3), sign} of
-// the normal components, in the reference's source order.
-// 3D slots 1..26 enumerate (dx, dy, dz) in x-, then y-, then z-major order
-// skipping the centre (GPU3D.cu:1492-1544).
-const int8_t kIc3[18][3] = {{3, 3, 1},  {1, 3, -1},  {6, 2, 1},   {9, 3, 1},   {7, 3, -1},  {4, 2, -1},
-                            {12, 2, 1}, {10, 2, -1}, {14, 1, 1},  {17, 2, 1},  {15, 2, -1}, {13, 1, -1},
-                            {20, 3, 1}, {18, 3, -1}, {23, 2, 1},  {26, 3, 1},  {24, 3, -1}, {21, 2, -1}};
-const int8_t kIr3[18][3] = {{9, 3, 1},  {2, 2, -1},  {3, 3, -1},  {1, 3, -1},  {8, 2, 1},   {7, 3, 1},
-                            {17, 2, 1}, {11, 1, -1}, {12, 2, -1}, {10, 2, -1}, {16, 1, 1},  {15, 2, 1},
-                            {26, 3, 1}, {19, 2, -1}, {20, 3, -1}, {18, 3, -1}, {25, 2, 1},  {24, 3, 1}};
-const int8_t kIl3[18][3] = {{18, 3, 1}, {19, 2, 1},  {20, 3, 1},  {21, 2, 1},  {22, 1, 1},  {23, 2, 1},
-                            {24, 3, 1}, {25, 2, 1},  {26, 3, 1},  {1, 3, -1},  {2, 2, -1},  {3, 3, -1},
-                            {4, 2, -1}, {5, 1, -1},  {6, 2, -1},  {7, 3, -1},  {8, 2, -1},  {9, 3, -1}};
-// 2D slots | 1 2 3 | 4 s 5 | 6 7 8 | with x to the right, y down (new_11.cu:1544-1565).
-const int8_t kIl2[6][3] = {{1, 2, -1}, {3, 2, 1}, {4, 1, -1}, {5, 1, 1}, {6, 2, -1}, {8, 2, 1}};
-const int8_t kIr2[6][3] = {{1, 2, -1}, {2, 1, -1}, {3, 2, -1}, {6, 2, 1}, {7, 1, 1}, {8, 2, 1}};
-const int kSlot2X[9] = {0, -1, 0, 1, -1, 1, -1, 0, 1};
-const int kSlot2Y[9] = {0, -1, -1, -1, 0, 0, 1, 1, 1};
+// Occupancy terms of the normal components (mirror_tables.h).
+const int8_t kIc3[18][3] = LQT_MIRROR_IC3;
+const int8_t kIr3[18][3] = LQT_MIRROR_IR3;
+const int8_t kIl3[18][3] = LQT_MIRROR_IL3;
+const int8_t kIl2[6][3] = LQT_MIRROR_IL2;
+const int8_t kIr2[6][3] = LQT_MIRROR_IR2;
+const int kSlot2X[9] = LQT_MIRROR_SLOT2X;
+const int kSlot2Y[9] = LQT_MIRROR_SLOT2Y;
 
 double occ_sum(const int8_t (*t)[3], int n, const int *gg)
 {

@@ -1,5 +1,7 @@
 // geometry.h -- host preprocessing of tissue grids (geometry.cc).
 #pragma once
+#include <cuda_runtime.h>
+
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -18,6 +20,9 @@ struct TissueMap {
 };
 
 int64_t build_tissue_map(int32_t nx, int32_t ny, int32_t nz, const uint8_t *types, TissueMap &out);
+// The same map built on the current device (k_geom.cu); returns an lqt status.
+int build_tissue_map_gpu(int32_t nx, int32_t ny, int32_t nz, const uint8_t *types_host, cudaStream_t st,
+                         TissueMap &out);
 void build_tensor(int32_t nx, int32_t ny, int32_t nz, double dx, const TissueMap &tm, const float *fibre,
                   double d_f, double d_t, std::vector<float> &d6, std::vector<float> &b3);
 

@@ -70,7 +70,20 @@ template <typename R> struct GridDev {
     // runs out; wait_limit = polls per wait (0 = the default limit)
     int32_t sub_skip_copy;
     uint32_t sub_wait_limit;
+    // V-halo staging of the 3D substep (variants 200 + CTAs/SM): per tile of
+    // kSubTile voxels the box of the dense V grid its 19-point stencils reach,
+    // as whole z-segments of its columns; vbox_hdr[8 per tile] = {ok, zlo,
+    // xlo, ylo, bx, by, bz, 0} (ok = 0: the box is larger than the stage, the
+    // tile reads V from the grid); vli[k] = the voxel's index in its box,
+    // ((x - xlo) * by + (y - ylo)) * bz + (z - zlo).  Null = not built.
+    const int32_t *vbox_hdr;
+    const int32_t *vli;
 };
+
+// Floats of a tile's V box in one stage of the staged substep (16 KB), and the
+// most columns (z-segment copies) a box may have.
+constexpr int kVBoxFloats = 4096;
+constexpr int kVBoxMaxCols = 64;
 
 // Voxels per tile of the staged substep kernel; the per-voxel arrays it
 // streams (control bytes, dense index, tensor, divergence, rate, detector
@@ -88,12 +101,15 @@ template <typename R>
 cudaError_t launch_grid_step_minb(const GridDev<R> &gd, const StepT<R> &k, int cur, int dim, int minb, cudaStream_t st);
 template <typename R> cudaError_t launch_ghost(const GridDev<R> &gd, int nxt, cudaStream_t st);
 // Variants of the V-only substep: minimum CTAs/SM of 256 threads of
-// k_sur_substep (5, 6, 8: one thread per voxel, direct loads) or of
+// k_sur_substep (5, 6, 8: one thread per voxel, direct loads), of
 // k_sur_substep_tile (100 + CTAs/SM: persistent CTAs, each tile's streamed
 // rows staged in shared memory by bulk asynchronous copies; 2D/3D
-// anisotropic grids, the others fall back to the direct kernel).
-constexpr int kSubVariants[6] = {5, 6, 8, 105, 106, 108};
-constexpr int kSubNVariants = 6;
+// anisotropic grids, the others fall back to the direct kernel) or of
+// k_sur_substep_vbox (200 + CTAs/SM: the same with each tile's V halo box
+// staged too; 3D anisotropic grids with nz a multiple of 4 and the boxes
+// built, the others fall back to k_sur_substep_tile at 5 CTAs/SM).
+constexpr int kSubVariants[8] = {5, 6, 8, 105, 106, 108, 203, 204};
+constexpr int kSubNVariants = 8;
 cudaError_t launch_sur_substep(const GridDev<float> &gd, double dt, int cur, int dim, int minb, cudaStream_t st);
 template <typename R>
 cudaError_t launch_ecg(const GridDev<R> &gd, int cur, const float4 *el, int nel, double *partial, double *out,

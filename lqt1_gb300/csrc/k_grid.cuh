@@ -247,13 +247,14 @@ template <int DIM> __device__ __forceinline__ void sub_tensor_unpack(const float
     if (DIM == 3) Bt[2] = q[4].x;
 }
 
+// The anisotropic stencil of grid_du with the tensor already loaded, on any
+// x-major array of V with strides sx, sy (z stride 1): the dense grid, or a
+// tile's box of it staged in shared memory (the same values in the same
+// order of operations, so the same bits).
 template <int DIM>
-__device__ __forceinline__ float sub_du(const GridDev<float> &gd, const float *__restrict__ V, int64_t g, int64_t k,
-                                        float vc, const float *Dt, const float *Bt)
+__device__ __forceinline__ float sub_du_at(const GridDev<float> &gd, const float *__restrict__ V, int64_t g,
+                                           int64_t sx, int64_t sy, float vc, const float *Dt, const float *Bt)
 {
-    if (DIM == 1 || !gd.d6) return grid_du<float, DIM>(gd, V, g, k, vc);
-    // the anisotropic stencil of grid_du with the tensor already loaded
-    const int64_t sx = gd.sx, sy = gd.sy;
     const float vxp = V[g + sx], vxm = V[g - sx], vyp = V[g + sy], vym = V[g - sy];
     const float c2 = gd.inv_dx2, c4 = gd.inv_4dx2, c1 = gd.inv_2dx;
     const float lxx = (vxp + vxm - 2.f * vc) * c2;
@@ -268,6 +269,14 @@ __device__ __forceinline__ float sub_du(const GridDev<float> &gd, const float *_
         du += Dt[2] * lzz + 2.f * (Dt[4] * lxz + Dt[5] * lyz) + Bt[2] * ((vzp - vzm) * c1);
     }
     return du;
+}
+
+template <int DIM>
+__device__ __forceinline__ float sub_du(const GridDev<float> &gd, const float *__restrict__ V, int64_t g, int64_t k,
+                                        float vc, const float *Dt, const float *Bt)
+{
+    if (DIM == 1 || !gd.d6) return grid_du<float, DIM>(gd, V, g, k, vc);
+    return sub_du_at<DIM>(gd, V, g, gd.sx, gd.sy, vc, Dt, Bt);
 }
 
 // MINB: minimum resident CTAs per SM (occupancy variants, picked at run time

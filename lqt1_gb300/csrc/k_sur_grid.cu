@@ -320,21 +320,22 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
             }
             elig = net_ok && fabsf(dv) <= sg.dvdt_max && !stim_ahead(gd, ck, ctl, k, sg.nsub);
         }
-        // 1. features (the previous tile's MMAs have all completed)
+        // 1. the state, loaded once: the features are built from it and the
+        //    coarse step advances it in registers while the first layer's
+        //    MMAs run
+        CellState<float> c;
+        if (elig) {
+            load_cell(c, gd.s, k);
+            c.v = vc;
+        }
         if (use_net) {
+            // features (the previous tile's MMAs have all completed)
             uint4 *row[kMlpIn / 8];
 #pragma unroll
             for (int j = 0; j < kMlpIn / 8; ++j) row[j] = reinterpret_cast<uint4 *>(xh + tc::kmaj_off(t, j * 8, kMlpIn));
             if (elig) {
-                const int64_t ld = gd.s.ld;
-                const float *cf = reinterpret_cast<const float *>(gd.s.conc);
                 float f[kMlpIn];
-                f[0] = vc;
-#pragma unroll
-                for (int j = 0; j < 8; ++j) f[1 + j] = cf[j * ld + k];
-                // gate slots in network order: all 31 but hsp, jp (3, 4)
-#pragma unroll
-                for (int j = 0; j < 29; ++j) f[9 + j] = gd.s.gate[(j < 3 ? j : j + 2) * ld + k];
+                state38(c, f);
                 f[38] = sg.par[0];
                 f[39] = sg.par[1];
                 f[40] = sg.par[2];
@@ -364,15 +365,24 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
         }
         tc::fence_before();            // previous tile's tcgen05.ld before the barrier
         const int any = wg_or(bar_id, elig ? 1 : 0);
-        // 2. the network
+        const bool run_net = use_net && any && net_ok;
+        if (run_net && t == 0) {
+            tc::fence_after();
+            gemm(t_acc_mma, xh, smem + kOffW1, kMlpIn, kMlpHid, smem + kOffOnes, smem + kOffB1, false);
+            tc::mma_commit(bar);
+        }
+        // 2. coarse TPORd step of the macro length, overlapping layer 1
+        if (elig) {
+            StepOut<float> o;
+            tpord_step<float>(c, ct, gd.model, sg.kmac, 0.f, 0.f, &o);
+        }
+        // 3. the rest of the network
         bool have_net = false;
-        if (use_net && any) {
+        if (run_net) {
             for (int layer = 0; layer < 3; ++layer) {
-                if (t == 0) {
+                if (layer > 0 && t == 0) {
                     tc::fence_after();
-                    if (layer == 0)
-                        gemm(t_acc_mma, xh, smem + kOffW1, kMlpIn, kMlpHid, smem + kOffOnes, smem + kOffB1, false);
-                    else if (layer == 1)
+                    if (layer == 1)
                         gemm(t_acc_mma, xh, smem + kOffW2, kMlpHid, kMlpHid, smem + kOffOnesH, smem + kOffB2, true);
                     else gemm(t_acc_mma, xh, smem + kOffW3, kMlpHid, kMlpOut, smem + kOffOnesH, smem + kOffB3, true);
                     tc::mma_commit(bar);
@@ -410,14 +420,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
             }
             have_net = net_ok;
         }
-        // 3. coarse step + correction
-        CellState<float> c;
-        if (elig) {
-            load_cell(c, gd.s, k);
-            c.v = vc;
-            StepOut<float> o;
-            tpord_step<float>(c, ct, gd.model, sg.kmac, 0.f, 0.f, &o);
-        }
+        // 4. the correction
         bool ok = elig && (net_ok || !use_net);
         uint32_t why = 0;   // failed checks: 1 network bound, 2 gate range, 4 concentration, 8 ionic V step
         if (have_net) {

@@ -127,6 +127,145 @@ __global__ void __launch_bounds__(kSubTile, MINB) k_sur_substep_tile(GridDev<flo
 
 namespace {
 
+// One stage of the V-halo kernel: the tile's streamed rows, each voxel's index
+// in the tile's V box, the box itself and the tile's box header.
+struct __align__(16) VStage {
+    SubStage rows;
+    int32_t li[kSubTile];
+    float vb[kVBoxFloats];
+    int32_t hdr[8];
+};
+static_assert(offsetof(VStage, li) % 16 == 0 && offsetof(VStage, vb) % 16 == 0 && sizeof(VStage) % 16 == 0,
+              "bulk copies need 16-byte aligned destinations");
+
+struct VHdr {
+    int32_t ok, zlo, xlo, ylo, bx, by, bz;
+};
+
+__device__ __forceinline__ VHdr vhdr_load(const int32_t *h)
+{
+    const int4 a = __ldg(reinterpret_cast<const int4 *>(h)), b = __ldg(reinterpret_cast<const int4 *>(h) + 1);
+    return VHdr{a.x, a.y, a.z, a.w, b.x, b.y, b.z};
+}
+
+// Thread 0: the rows, box indices and (when the box fits) the V box of tile
+// k0 / kSubTile into one stage, completing on bar.  The box's columns are
+// z-segments [zlo, zlo + bz) of the dense grid, each copied whole: nz, zlo
+// and bz are multiples of 4, so every source and destination is 16-byte
+// aligned and every size a multiple of 16 bytes; the host builder keeps every
+// segment inside its column (zlo + bz <= nz) and every column inside the grid.
+__device__ __forceinline__ void vbox_issue(VStage &st, uint64_t *bar, const GridDev<float> &gd, const float *V,
+                                           int64_t k0, bool det, const VHdr &h)
+{
+    constexpr uint32_t n = kSubTile;
+    const uint32_t box = h.ok ? (uint32_t)(h.bx * h.by * h.bz) * 4u : 0u;
+    tc::mbar_expect_tx(bar, n * (4 + 4 + 12 + 8 + 1) + (det ? n : 0) + n * 4 + box);
+    tc::bulk_g2s(st.rows.rate, gd.srate + k0, n * 4, bar);
+    tc::bulk_g2s(st.rows.gidx, gd.gidx + k0, n * 4, bar);
+    tc::bulk_g2s(st.rows.d6, gd.d6h + 3 * k0, n * 12, bar);
+    tc::bulk_g2s(st.rows.b3, gd.b3h + 2 * k0, n * 8, bar);
+    tc::bulk_g2s(st.rows.ctl, gd.ctl + k0, n, bar);
+    if (det) tc::bulk_g2s(st.rows.flag, gd.sdflag + k0, n, bar);
+    tc::bulk_g2s(st.li, gd.vli + k0, n * 4, bar);
+    if (h.ok) {
+        const int64_t ny = gd.sx / gd.sy, nz = gd.sy;
+        for (int i = 0; i < h.bx; ++i)
+            for (int j = 0; j < h.by; ++j)
+                tc::bulk_g2s(st.vb + (i * h.by + j) * h.bz, V + ((int64_t)(h.xlo + i) * ny + (h.ylo + j)) * nz + h.zlo,
+                             (uint32_t)h.bz * 4u, bar);
+    }
+    st.hdr[0] = h.ok;
+    st.hdr[1] = h.by * h.bz;
+    st.hdr[2] = h.bz;
+}
+
+}  // namespace
+
+// 3D V-only substep with the V halo staged: persistent CTAs, two stages; each
+// stage holds a tile's streamed rows and the box of the dense V grid its
+// stencils reach, brought by bulk asynchronous copies issued two tiles ahead,
+// so the threads read the 19-point stencil from shared memory.  A tile whose
+// box exceeds the stage reads V from the grid.  Arithmetic identical to
+// k_sur_substep.  Waits and their failure path as in k_sur_substep_tile.
+template <int MINB>
+__global__ void __launch_bounds__(kSubTile, MINB) k_sur_substep_vbox(GridDev<float> gd, float dt, int cur)
+{
+    extern __shared__ __align__(128) uint8_t vsm[];
+    VStage *stg = reinterpret_cast<VStage *>(vsm);
+    __shared__ __align__(8) uint64_t bar[2];
+    const int t = threadIdx.x;
+    const int64_t ntiles = (gd.ntissue + kSubTile - 1) / kSubTile;
+    const int64_t stride = gridDim.x;
+    int64_t tile = blockIdx.x;
+    if (tile >= ntiles) return;
+    const bool det = gd.det != nullptr;
+    const uint32_t lim = gd.sub_wait_limit ? gd.sub_wait_limit : kSubWaitLimit;
+    const float *__restrict__ V = gd.vg[cur];
+    float *__restrict__ Vn = gd.vg[cur ^ 1];
+    VHdr hnext{};       // thread 0: header of the tile two ahead
+    if (t == 0) {
+        tc::mbar_init(&bar[0], 1);
+        tc::mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        if (!gd.sub_skip_copy) vbox_issue(stg[0], &bar[0], gd, V, tile * kSubTile, det, vhdr_load(gd.vbox_hdr + 8 * tile));
+        if (tile + stride < ntiles)
+            vbox_issue(stg[1], &bar[1], gd, V, (tile + stride) * kSubTile, det,
+                       vhdr_load(gd.vbox_hdr + 8 * (tile + stride)));
+    }
+    __syncthreads();
+    const Clock ck = *gd.clk;
+    for (uint32_t it = 0; tile < ntiles; tile += stride, ++it) {
+        const int s = it & 1;
+        if (t == 0 && tile + 2 * stride < ntiles) hnext = vhdr_load(gd.vbox_hdr + 8 * (tile + 2 * stride));
+        const bool ok = tc::mbar_wait(&bar[s], (it >> 1) & 1, lim);
+        if (!__syncthreads_and(ok ? 1 : 0)) {
+            if (t == 0) {
+                atomicOr(gd.serr, 2);
+                if (it > 0 || !gd.sub_skip_copy) tc::mbar_wait(&bar[s], (it >> 1) & 1, kSubWaitLimit);
+                if (tile + stride < ntiles) tc::mbar_wait(&bar[s ^ 1], ((it + 1) >> 1) & 1, kSubWaitLimit);
+            }
+            return;
+        }
+        const VStage &st = stg[s];
+        const SubStage &sg = st.rows;
+        const int64_t k = tile * kSubTile + t;
+        const float r = sg.rate[t];
+        if (k < gd.ntissue && r == r) {
+            const int64_t g = sg.gidx[t];
+            float2 q[5];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) q[i] = __half22float2(sg.d6[3 * t + i]);
+#pragma unroll
+            for (int i = 0; i < 2; ++i) q[3 + i] = __half22float2(sg.b3[2 * t + i]);
+            float Dt[6], Bt[3];
+            sub_tensor_unpack<3>(q, Dt, Bt);
+            float vc, du;
+            if (st.hdr[0]) {
+                const int64_t li = st.li[t];
+                vc = st.vb[li];
+                du = sub_du_at<3>(gd, st.vb, li, st.hdr[1], st.hdr[2], vc, Dt, Bt);
+            } else {
+                vc = V[g];
+                du = sub_du_at<3>(gd, V, g, gd.sx, gd.sy, vc, Dt, Bt);
+            }
+            const float ist = grid_stim(gd, ck, sg.ctl[t], k);
+            const float dvdt = r - ist;
+            const float vn = vc + (dvdt + du) * dt;
+            Vn[g] = vn;
+            if (det && sg.flag[t]) grid_detect(gd, ck, k, vc, vn, dvdt);
+            const bool bad = !(vn == vn) || vn < gd.vmin_ok || vn > gd.vmax_ok;
+            if (bad) atomicAdd(gd.nbad, 1ull);
+        }
+        __syncthreads();   // every thread is done with stage s
+        if (t == 0 && tile + 2 * stride < ntiles) {
+            tc::fence_proxy_async();
+            vbox_issue(stg[s], &bar[s], gd, V, (tile + 2 * stride) * kSubTile, det, hnext);
+        }
+    }
+}
+
+namespace {
+
 template <int MINB> void launch_minb(const GridDev<float> &gd, double dt, int cur, int dim, unsigned nb, cudaStream_t st)
 {
     if (dim == 1) k_sur_substep<1, MINB><<<nb, 256, 0, st>>>(gd, (float)dt, cur);
@@ -162,6 +301,22 @@ template <int DIM, int MINB> cudaError_t launch_tile(const GridDev<float> &gd, d
     return cudaGetLastError();
 }
 
+template <int MINB> cudaError_t launch_vbox(const GridDev<float> &gd, double dt, int cur, cudaStream_t st)
+{
+    static std::atomic<uint64_t> done{0}, carve{0};
+    const uint32_t bytes = 2 * sizeof(VStage);
+    cudaError_t e = tc::smem_attr_once(k_sur_substep_vbox<MINB>, bytes, done);
+    if (e == cudaSuccess) e = carveout_once(k_sur_substep_vbox<MINB>, carve);
+    if (e != cudaSuccess) return e;
+    int dev = 0, nsm = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t ntiles = (gd.ntissue + kSubTile - 1) / kSubTile;
+    const int64_t grid = ntiles < (int64_t)nsm * MINB ? ntiles : (int64_t)nsm * MINB;
+    k_sur_substep_vbox<MINB><<<(unsigned)grid, kSubTile, bytes, st>>>(gd, (float)dt, cur);
+    return cudaGetLastError();
+}
+
 bool al16(const void *p) { return p && ((uintptr_t)p & 15u) == 0; }
 
 }  // namespace
@@ -169,6 +324,13 @@ bool al16(const void *p) { return p && ((uintptr_t)p & 15u) == 0; }
 cudaError_t launch_sur_substep(const GridDev<float> &gd, double dt, int cur, int dim, int variant, cudaStream_t st)
 {
     if (gd.ntissue <= 0) return cudaSuccess;
+    if (variant >= 200) {
+        if (dim == 3 && gd.d6 && gd.vbox_hdr && gd.vli && al16(gd.vli) && al16(gd.d6h) && al16(gd.b3h) &&
+            al16(gd.srate) && al16(gd.gidx) && al16(gd.ctl) && al16(gd.vg[0]) && al16(gd.vg[1]) && gd.serr &&
+            (!gd.det || al16(gd.sdflag)))
+            return variant == 203 ? launch_vbox<3>(gd, dt, cur, st) : launch_vbox<4>(gd, dt, cur, st);
+        variant = 105;
+    }
     const bool tile = variant >= 100;
     const int minb = tile ? variant - 100 : variant;
     if (dim >= 2 && gd.d6 && !(gd.d6h && gd.b3h)) return cudaErrorInvalidValue;   // FP16 tensor copies missing

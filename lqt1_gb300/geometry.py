@@ -38,6 +38,8 @@ def _bind():
     L.lqt_geom_ventricle.restype = C.c_int
     L.lqt_geom_mirror_map.argtypes = [C.c_int32, C.c_int32, C.c_int32, P, P, P, P, C.POINTER(C.c_int64)]
     L.lqt_geom_mirror_map.restype = C.c_int
+    L.lqt_geom_mirror_map_gpu.argtypes = [C.c_int32, C.c_int32, C.c_int32, P, P, P, P, C.POINTER(C.c_int64), P]
+    L.lqt_geom_mirror_map_gpu.restype = C.c_int
     return L
 
 
@@ -87,17 +89,23 @@ def ventricle(nx=320, ny=320, nz=420, dx=0.2, a_out=25.0, c_out=62.0, wall=10.0,
     return Ventricle(t, f, m, isl, sp)
 
 
-def mirror_map(types: np.ndarray):
-    """(tissue_of, bnd_dst, bnd_src) of a grid, as lqt_sim_create builds them."""
+def mirror_map(types: np.ndarray, gpu: bool = False):
+    """(tissue_of, bnd_dst, bnd_src) of a grid: built on the host
+    (lqt_geom_mirror_map) or on the GPU as lqt_sim_create builds them
+    (lqt_geom_mirror_map_gpu); the two are bit-identical."""
     L = _bind()
     g = np.ascontiguousarray(types, dtype=np.uint8)
     shp = g.shape + (1,) * (3 - g.ndim)
     tissue_of = np.zeros(g.size, np.int32)
     n = C.c_int64()
-    N.check(L.lqt_geom_mirror_map(*shp, _p(g), None, None, None, C.byref(n)), "lqt_geom_mirror_map")
+    if gpu:
+        call = lambda *a: L.lqt_geom_mirror_map_gpu(*a, None)  # noqa: E731
+    else:
+        call = L.lqt_geom_mirror_map
+    N.check(call(*shp, _p(g), None, None, None, C.byref(n)), "lqt_geom_mirror_map")
     dst = np.zeros(n.value, np.int64)
     src = np.zeros(n.value, np.int64)
-    N.check(L.lqt_geom_mirror_map(*shp, _p(g), _p(tissue_of), _p(dst), _p(src), C.byref(n)), "lqt_geom_mirror_map")
+    N.check(call(*shp, _p(g), _p(tissue_of), _p(dst), _p(src), C.byref(n)), "lqt_geom_mirror_map")
     return tissue_of, dst, src
 
 

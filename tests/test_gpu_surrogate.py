@@ -272,10 +272,12 @@ def test_speed_gain_over_plain_step(lq, torch, net):
 @pytest.mark.parametrize("dim", [2, 3])
 def test_substep_variants_bit_identical(lq, net, dim):
     """Every kernel of the V-only substep (direct loads at 5 and 8 CTAs/SM;
-    tiles staged in shared memory by bulk copies at 5, 6 and 8 CTAs/SM) gives
-    the same bits: state, V, detector and surrogate counters after the
-    upstroke and into the plateau of an anisotropic grid whose voxel count is
-    not a multiple of the 256-voxel tile."""
+    tiles staged in shared memory by bulk copies at 5, 6 and 8 CTAs/SM; in 3D
+    also the tiles' V halo boxes staged, at 3 and 4 CTAs/SM) gives the same
+    bits: state, V, detector and surrogate counters after the upstroke and
+    into the plateau of an anisotropic grid whose voxel count is not a
+    multiple of the 256-voxel tile (3D: nz = 52, a multiple of 4, so the V
+    boxes are built)."""
     if dim == 2:
         sh = lq.geometry.sheet(130, 97, s1_cols=3)
         nx, ny = sh.types.shape
@@ -283,12 +285,12 @@ def test_substep_variants_bit_identical(lq, net, dim):
         fibre = np.stack([np.cos(ang), np.sin(ang), np.zeros_like(ang)], -1).astype(np.float32)
         types, mask, dx = sh.types, sh.s1_mask, 0.15
     else:
-        v = lq.geometry.ventricle(nx=44, ny=44, nz=50, dx=0.2, a_out=4.0, c_out=8.0, wall=2.0, z_base=9.0,
+        v = lq.geometry.ventricle(nx=44, ny=44, nz=52, dx=0.2, a_out=4.0, c_out=8.0, wall=2.0, z_base=9.0,
                                   island_radius=1.5, stim_radius=1.2)
         types, fibre, mask, dx = v.types, v.fibre, v.s1_mask, 0.2
     m = lq.model("baseline", gks_scale=0.5, pca_scale=1.5, gks_iso_scale=1.2)
     out = {}
-    for var in (5, 8, 105, 106, 108):
+    for var in (5, 8, 105, 106, 108) + ((203, 204) if dim == 3 else ()):
         sim = lq.Sim(types, dx, fibre=fibre, precision=lq.MIXED, model=m)
         assert sim.n % 256 != 0
         sim.set_protocol(bcl=1000.0, s1_mask=mask, s1_start=0.0, s1_duration=2.0, s1_strength=-52.0)
