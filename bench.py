@@ -362,6 +362,8 @@ def main():
     if args.only:
         prec = lq.FP64 if args.only == "fp64" else lq.MIXED
         so = make_sim(prec, args.only == "surrogate")
+        if args.only == "surrogate" and args.substep_variant >= 0:
+            so.substep_variant(args.substep_variant)
         so.step(args.prerun)
         ms_o = timed(so, args.steps)
         print(json.dumps({"only": args.only, "workload": w["desc"], "steps": args.steps, "ms": ms_o,
