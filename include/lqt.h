@@ -369,12 +369,15 @@ int lqt_sim_tune(lqt_sim *s, int32_t variant, int32_t *chosen, float *ms_per_var
  * elsewhere the direct kernel runs); 203, 204 = the same with each tile's
  * V halo (the box of the dense V grid its 19-point stencils reach, copied as
  * z-segments of its columns) staged in shared memory too, at 3, 4 CTAs/SM
- * (3D anisotropic grids with nz a multiple of 4; elsewhere 105 runs).
- * variant >= 0 forces one (the autotuner then keeps it); variant < 0 only
- * reports the current one.  All variants give bit-identical results.
- * ms_per_variant (or NULL): 8 mean milliseconds per step from the last
- * autotune, in the order 5, 6, 8, 105, 106, 108, 203, 204 (zeros if it has not
- * run). */
+ * (3D anisotropic grids with nz a multiple of 4; elsewhere 105 runs);
+ * 304, 305, 306 = one producer warp streams each tile's rows into a two-stage
+ * shared-memory ring (full/empty barriers) while eight warps compute, V read
+ * from the grid, at 4, 5, 6 CTAs/SM (2D/3D anisotropic grids; elsewhere 105
+ * runs).  variant >= 0 forces one (the autotuner then keeps it); variant < 0
+ * only reports the current one.  All variants give bit-identical results.
+ * ms_per_variant (or NULL): 11 mean milliseconds per step from the last
+ * autotune, in the order 5, 6, 8, 105, 106, 108, 203, 204, 304, 305, 306
+ * (zeros if it has not run). */
 int lqt_sim_substep_variant(lqt_sim *s, int32_t variant, int32_t *chosen, float *ms_per_variant);
 
 /* Instrumentation (no counterpart in the reference, which has no timing):
@@ -556,7 +559,9 @@ int lqt_mlp_train_step(lqt_mlp *m, const void *x_bf16_dev, const float *t_dev,
  * from the same start (the correction the network learns).  Macro steps that are not
  * recorded carry a seeded constant current uniform in +-jitter pA/pF, which
  * moves the cells off the single-cell trajectory as tissue coupling does.
- * Up to cap rows; *count = rows written. */
+ * Up to cap rows; *count = rows written.  The rows are in cell order (cell
+ * after cell, each cell's pairs in time order; a set longer than cap keeps the
+ * first cells), so the same arguments give the same bits on every run. */
 typedef struct lqt_sur_ranges {
     double gks[2], pca[2], iso[2], bcl[2];
     int32_t beats_warm, beats_record;

@@ -46,6 +46,7 @@ struct lqt_mlp {
     int64_t ws_batch = 0;
     float *Z1 = nullptr, *Z2 = nullptr, *Y = nullptr;
     __nv_bfloat16 *H1 = nullptr, *H2 = nullptr, *dY = nullptr, *dZ1 = nullptr, *dZ2 = nullptr;
+    float *Gpart = nullptr;         // split-K slices of the weight gradients (ordered reduction)
     DevMem ws;
     MlpDev dev() const
     {
@@ -76,6 +77,9 @@ static int upload_params(lqt_mlp *m, const std::vector<float> &p)
     return LQT_OK;
 }
 
+// K slices of the weight-gradient GEMMs (K = batch): about 256 rows each.
+static int splitk_for(int64_t B) { return (int)std::min<int64_t>(128, std::max<int64_t>(1, B / 256)); }
+
 static int ensure_ws(lqt_mlp *m, int64_t B)
 {
     if (B <= m->ws_batch) return LQT_OK;
@@ -83,7 +87,9 @@ static int ensure_ws(lqt_mlp *m, int64_t B)
     int rc = m->ws.alloc((void **)&m->Z1, B * kMlpHid * 4) | m->ws.alloc((void **)&m->Z2, B * kMlpHid * 4) |
              m->ws.alloc((void **)&m->Y, B * kMlpOut * 4) | m->ws.alloc((void **)&m->H1, B * kMlpHid * 2) |
              m->ws.alloc((void **)&m->H2, B * kMlpHid * 2) | m->ws.alloc((void **)&m->dY, B * kMlpOut * 2) |
-             m->ws.alloc((void **)&m->dZ1, B * kMlpHid * 2) | m->ws.alloc((void **)&m->dZ2, B * kMlpHid * 2);
+             m->ws.alloc((void **)&m->dZ1, B * kMlpHid * 2) | m->ws.alloc((void **)&m->dZ2, B * kMlpHid * 2) |
+             m->ws.alloc((void **)&m->Gpart,
+                         (int64_t)std::max(1, gemm_splitk_slices((int)B, splitk_for(B))) * kMlpHid * kMlpHid * 4);
     if (rc) return LQT_ERR_NOMEM;
     m->ws_batch = B;
     return LQT_OK;
@@ -141,17 +147,17 @@ static int forward_backward(lqt_mlp *m, const __nv_bfloat16 *X, const float *T, 
     g.err = m->err;
     CK(launch_gemm_bf16(g, st));
     CK(cudaMemsetAsync(m->G, 0, kNParam * 4, st));
-    const int ks = (int)std::min<int64_t>(128, std::max<int64_t>(1, B / 256));
+    const int ks = splitk_for(B);
     g = gemm(m->dY, kMlpOut, 1, m->H2, kMlpHid, 0, kMlpOut, kMlpHid, b);
-    g.epi = kEpiAtomic; g.C = m->G + kOW3; g.ksplit = ks;
+    g.epi = kEpiAtomic; g.C = m->G + kOW3; g.ksplit = ks; g.partial = m->Gpart;
     g.err = m->err;
     CK(launch_gemm_bf16(g, st));
     g = gemm(m->dZ2, kMlpHid, 1, m->H1, kMlpHid, 0, kMlpHid, kMlpHid, b);
-    g.epi = kEpiAtomic; g.C = m->G + kOW2; g.ksplit = ks;
+    g.epi = kEpiAtomic; g.C = m->G + kOW2; g.ksplit = ks; g.partial = m->Gpart;
     g.err = m->err;
     CK(launch_gemm_bf16(g, st));
     g = gemm(m->dZ1, kMlpHid, 1, X, kMlpIn, 0, kMlpHid, kMlpIn, b);
-    g.epi = kEpiAtomic; g.C = m->G + kOW1; g.ksplit = ks;
+    g.epi = kEpiAtomic; g.C = m->G + kOW1; g.ksplit = ks; g.partial = m->Gpart;
     g.err = m->err;
     CK(launch_gemm_bf16(g, st));
     CK(launch_colsum(m->dY, B, kMlpOut, m->G + kOB3, st));
@@ -344,20 +350,30 @@ int lqt_sur_datagen(int64_t ncells, uint64_t seed, const lqt_sur_ranges *r, floa
     DevMem tmp;
     SurCell *dc = nullptr;
     ModelK *dm = nullptr;
-    unsigned long long *cnt = nullptr;
+    int64_t *per_cell = nullptr;
     if (tmp.alloc((void **)&dc, ncells * sizeof(SurCell)) | tmp.alloc((void **)&dm, ncells * sizeof(ModelK)) |
-        tmp.alloc((void **)&cnt, 16))
+        tmp.alloc((void **)&per_cell, ncells * sizeof(int64_t)))
         return LQT_ERR_NOMEM;
     cudaStream_t st = (cudaStream_t)stream;
     CK(cudaMemcpyAsync(dc, cells.data(), ncells * sizeof(SurCell), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(dm, models.data(), ncells * sizeof(ModelK), cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(cnt, 0, 8, st));
-    CK(launch_sur_datagen(dc, ncells, dm, make_stepk(r->dt), make_stepk(nsub * r->dt), x_dev, d_dev, cnt, cap,
-                          seed, (float)r->dvdt_max, (float)r->prob, (float)r->jitter, nsub, st));
-    unsigned long long c = 0;
-    CK(cudaMemcpyAsync(&c, cnt, 8, cudaMemcpyDeviceToHost, st));
+    // pass 1: pairs per cell; rows in cell order; pass 2: the pairs at their rows
+    CK(launch_sur_datagen(dc, ncells, dm, make_stepk(r->dt), make_stepk(nsub * r->dt), nullptr, nullptr, per_cell,
+                          nullptr, cap, seed, (float)r->dvdt_max, (float)r->prob, (float)r->jitter, nsub, st));
+    std::vector<int64_t> off(ncells);
+    CK(cudaMemcpyAsync(off.data(), per_cell, ncells * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    *count = (int64_t)std::min<unsigned long long>(c, (unsigned long long)cap);
+    int64_t total = 0;
+    for (int64_t i = 0; i < ncells; ++i) {
+        const int64_t c = off[i];
+        off[i] = total;
+        total += c;
+    }
+    CK(cudaMemcpyAsync(per_cell, off.data(), ncells * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    CK(launch_sur_datagen(dc, ncells, dm, make_stepk(r->dt), make_stepk(nsub * r->dt), x_dev, d_dev, nullptr,
+                          per_cell, cap, seed, (float)r->dvdt_max, (float)r->prob, (float)r->jitter, nsub, st));
+    CK(cudaStreamSynchronize(st));
+    *count = std::min<int64_t>(total, cap);
     return LQT_OK;
 }
 

@@ -107,9 +107,11 @@ template <typename R> cudaError_t launch_ghost(const GridDev<R> &gd, int nxt, cu
 // anisotropic grids, the others fall back to the direct kernel) or of
 // k_sur_substep_vbox (200 + CTAs/SM: the same with each tile's V halo box
 // staged too; 3D anisotropic grids with nz a multiple of 4 and the boxes
-// built, the others fall back to k_sur_substep_tile at 5 CTAs/SM).
-constexpr int kSubVariants[8] = {5, 6, 8, 105, 106, 108, 203, 204};
-constexpr int kSubNVariants = 8;
+// built, the others fall back to k_sur_substep_tile at 5 CTAs/SM) or of the
+// same producer-warp kernel with the rows only (300 + CTAs/SM; 2D/3D
+// anisotropic grids, the others fall back as the 100s do).
+constexpr int kSubVariants[11] = {5, 6, 8, 105, 106, 108, 203, 204, 304, 305, 306};
+constexpr int kSubNVariants = 11;
 cudaError_t launch_sur_substep(const GridDev<float> &gd, double dt, int cur, int dim, int minb, cudaStream_t st);
 template <typename R>
 cudaError_t launch_ecg(const GridDev<R> &gd, int cur, const float4 *el, int nel, double *partial, double *out,

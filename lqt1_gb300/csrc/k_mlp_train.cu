@@ -4,6 +4,8 @@
 // the loss gradient and the Adam update.  Training runs once, off the
 // simulation's hot path; the per-macro-step inference uses the tcgen05 kernel
 // in k_sur_grid.cu / k_mlp_tc.cu.
+#include <algorithm>
+
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -26,9 +28,27 @@ constexpr uint32_t kOffA = 0;
 constexpr uint32_t kOffB = kOffA + kTM * kKC * 2;
 constexpr uint32_t kOffBar = kOffB + kMaxN * kKC * 2;
 constexpr uint32_t kSmemBytes = 60 * 1024;
+constexpr int kEpPitch = 33;               // epilogue slab row pitch (floats): no bank conflicts
 static_assert(kOffBar + 16 <= kSmemBytes, "shared memory plan");
+static_assert(kTM * kEpPitch * 4 <= kOffBar, "epilogue slab fits the staging buffers");
 
 __device__ __forceinline__ float sigm(float z) { return 1.0f / (1.0f + __expf(-z)); }
+
+// K per slice of a split-K GEMM: whole staging chunks.
+__host__ __device__ inline int splitk_chunk(int K, int ksplit)
+{
+    return ((K + ksplit - 1) / ksplit + kKC - 1) / kKC * kKC;
+}
+
+// C[o] += the split-K slices of element o, added in slice order.
+__global__ void k_splitk_reduce(const float *__restrict__ partial, int64_t mn, int slices, float *__restrict__ C)
+{
+    for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < mn; o += (int64_t)gridDim.x * blockDim.x) {
+        float acc = 0.f;
+        for (int z = 0; z < slices; ++z) acc += partial[(int64_t)z * mn + o];
+        C[o] += acc;
+    }
+}
 
 // One 8-element K chunk of row r of op(X) (X[r][k] = ta ? src[k * ld + r] :
 // src[r * ld + k]) for k = k0 .. k0 + 7, zero outside rows < R and k < kend.
@@ -71,10 +91,12 @@ __global__ void __launch_bounds__(128) k_gemm_tc(GemmArgs g)
     while ((int)ncols < npad) ncols <<= 1;
     int kbeg = 0, kend = g.K;
     if (g.epi == kEpiAtomic && g.ksplit > 1) {
-        const int chunk = ((g.K + g.ksplit - 1) / g.ksplit + kKC - 1) / kKC * kKC;
+        const int chunk = splitk_chunk(g.K, g.ksplit);
         kbeg = blockIdx.z * chunk;
         kend = min(g.K, kbeg + chunk);
     }
+    // this CTA's slice of a split-K GEMM with a workspace: plain stores
+    float *const slab = (g.epi == kEpiAtomic && g.partial) ? g.partial + (int64_t)blockIdx.z * g.M * g.N : nullptr;
     if (tid == 0) {
         tc::mbar_init(bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -127,18 +149,24 @@ __global__ void __launch_bounds__(128) k_gemm_tc(GemmArgs g)
         __syncthreads();
     }
     if (ok && nchunk > 0) {
-        const int m = m0 + tid;
+        // epilogue in 32-column slabs: each thread moves its row (TMEM lane)
+        // into shared memory, then every warp writes whole row segments, so
+        // the stores (or atomics) of a warp are 32 consecutive elements
+        float *ep = reinterpret_cast<float *>(smem);          // the staging buffers are free now
         const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-        for (int n0 = 0; n0 < g.N; n0 += 16) {
-            float v[16];
-            tc::tmem_ld16(taddr + n0, v);              // whole warp
-            if (m >= g.M) continue;
+        const int lane = tid & 31;
+        for (int n0 = 0; n0 < g.N; n0 += 32) {
+            float v[32];
+            tc::tmem_ld32(taddr + n0, v);                     // whole warp
 #pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                const int n = n0 + i;
-                if (n >= g.N) break;
+            for (int i = 0; i < 32; ++i) ep[tid * kEpPitch + i] = v[i];
+            __syncthreads();
+            const int n = n0 + lane;
+            for (int r = warp; r < kTM; r += 4) {
+                const int m = m0 + r;
+                if (m >= g.M || n >= g.N) continue;
                 const int64_t o = (int64_t)m * g.N + n;
-                float x = v[i];
+                float x = ep[r * kEpPitch + lane];
                 if (g.epi == kEpiStore) {
                     if (g.bias) x += g.bias[n];
                     if (g.C) g.C[o] = x;
@@ -146,10 +174,13 @@ __global__ void __launch_bounds__(128) k_gemm_tc(GemmArgs g)
                 } else if (g.epi == kEpiDact) {
                     const float z = g.Z[o], sz = sigm(z);
                     g.Cb[o] = __float2bfloat16(x * (sz + z * sz * (1.0f - sz)));
+                } else if (slab) {
+                    slab[o] = x;
                 } else {
                     atomicAdd(&g.C[o], x);
                 }
             }
+            __syncthreads();
         }
     }
     tc::fence_before();
@@ -166,9 +197,26 @@ cudaError_t launch_gemm_bf16(const GemmArgs &g, cudaStream_t st)
     static std::atomic<uint64_t> attr_done{0};
     cudaError_t e = tc::smem_attr_once(k_gemm_tc, kSmemBytes, attr_done);
     if (e != cudaSuccess) return e;
-    dim3 grid(1, (g.M + kTM - 1) / kTM, g.epi == kEpiAtomic && g.ksplit > 1 ? g.ksplit : 1);
+    const int slices = gemm_splitk_slices(g.K, g.epi == kEpiAtomic ? g.ksplit : 1);
+    dim3 grid(1, (g.M + kTM - 1) / kTM, slices > 0 ? slices : 1);
     k_gemm_tc<<<grid, 128, kSmemBytes, st>>>(g);
-    return cudaGetLastError();
+    e = cudaGetLastError();
+    if (e == cudaSuccess && slices > 0 && g.partial) {
+        const int64_t mn = (int64_t)g.M * g.N;
+        k_splitk_reduce<<<(unsigned)std::min<int64_t>((mn + 255) / 256, 1024), 256, 0, st>>>(g.partial, mn, slices,
+                                                                                            g.C);
+        e = cudaGetLastError();
+    }
+    return e;
+}
+
+// Only slices that hold at least one chunk of K are launched, so every slice
+// of the workspace is written before the reduction reads it.
+int gemm_splitk_slices(int K, int ksplit)
+{
+    if (ksplit <= 1 || K <= 0) return 0;
+    const int chunk = splitk_chunk(K, ksplit);
+    return (K + chunk - 1) / chunk;
 }
 
 // ---- loss gradient and Adam -------------------------------------------------

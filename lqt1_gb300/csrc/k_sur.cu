@@ -35,12 +35,19 @@ __device__ __forceinline__ void sur_init_cell(CellState<float> &c)
 // state after one coarse step of the macro length from the same start.
 // Macro steps that are not recorded carry a constant current uniform in
 // +-jitter (a stand-in for the electrotonic load of tissue).
+// Two passes make the pair set and its order independent of thread timing:
+// with counts != NULL the kernel only counts each cell's recorded macro steps;
+// with offsets != NULL the j-th pair of cell i goes to row offsets[i] + j
+// (rows at or past cap are dropped, so a truncated set keeps the first cells
+// in cell order).  A cell's trajectory is the same in both passes: a macro
+// step chosen for recording carries no jitter current whether or not its row
+// is kept.
 __global__ void __launch_bounds__(128) k_sur_datagen(const SurCell *__restrict__ cells, int64_t ncells,
                                                      const ModelK *__restrict__ models, StepT<float> k,
                                                      StepT<float> kmac, float *__restrict__ X,
-                                                     float *__restrict__ D, unsigned long long *__restrict__ counter,
-                                                     int64_t cap, uint64_t seed, float dvdt_max, float prob,
-                                                     float jitter, int nsub)
+                                                     float *__restrict__ D, int64_t *__restrict__ counts,
+                                                     const int64_t *__restrict__ offsets, int64_t cap, uint64_t seed,
+                                                     float dvdt_max, float prob, float jitter, int nsub)
 {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= ncells) return;
@@ -51,7 +58,7 @@ __global__ void __launch_bounds__(128) k_sur_datagen(const SurCell *__restrict__
     const int ct = sc.ctype;
     const int cls = sur_class(ct);
     StepOut<float> o{};
-    int64_t slot = -1;
+    int64_t slot = -1, nrec = 0;
     float xc[kMlpNState];   // coarse end state (hi parts) of the pending sample
     float loc[8];           // and its concentration lo parts
     float ipert = 0.f;
@@ -76,9 +83,10 @@ __global__ void __launch_bounds__(128) k_sur_datagen(const SurCell *__restrict__
             ipert = 0.f;
             if (st >= sc.warm_steps && !stim_ahead && fabsf(o.dvdt) <= dvdt_max && st + nsub <= sc.nsteps &&
                 (sur_hash(seed, (uint64_t)i, (uint64_t)st) & 0xFFFFFF) < (uint32_t)(prob * 16777216.f)) {
-                const unsigned long long s = atomicAdd(counter, 1ull);
-                if (s < (unsigned long long)cap) {
-                    slot = (int64_t)s;
+                const int64_t s = counts ? -1 : offsets[i] + nrec;
+                ++nrec;
+                if (s >= 0 && s < cap) {
+                    slot = s;
                     float x0[kMlpNState];
                     state38(c, x0);
                     float *xr = X + slot * kSurFeat;
@@ -107,6 +115,7 @@ __global__ void __launch_bounds__(128) k_sur_datagen(const SurCell *__restrict__
         const float ist = (ph >= sc.stim_on && ph < sc.stim_off) ? sc.stim : (slot >= 0 ? 0.f : ipert);
         tpord_step<float>(c, ct, m, k, ist, 0.f, &o);
     }
+    if (counts) counts[i] = nrec;
 }
 
 // Raw features (kSurFeat floats per row) -> normalised BF16 network inputs
@@ -130,13 +139,14 @@ __global__ void k_sur_prepare(const float *__restrict__ X, const float *__restri
 }
 
 cudaError_t launch_sur_datagen(const SurCell *cells, int64_t ncells, const ModelK *models, const StepK &k,
-                               const StepK &kmac, float *X, float *D, unsigned long long *counter, int64_t cap,
-                               uint64_t seed, float dvdt_max, float prob, float jitter, int nsub, cudaStream_t st)
+                               const StepK &kmac, float *X, float *D, int64_t *counts, const int64_t *offsets,
+                               int64_t cap, uint64_t seed, float dvdt_max, float prob, float jitter, int nsub,
+                               cudaStream_t st)
 {
     if (ncells <= 0) return cudaSuccess;
     k_sur_datagen<<<(unsigned)((ncells + 127) / 128), 128, 0, st>>>(cells, ncells, models, step_as<float>(k),
-                                                                    step_as<float>(kmac), X, D, counter, cap, seed,
-                                                                    dvdt_max, prob, jitter, nsub);
+                                                                    step_as<float>(kmac), X, D, counts, offsets, cap,
+                                                                    seed, dvdt_max, prob, jitter, nsub);
     return cudaGetLastError();
 }
 

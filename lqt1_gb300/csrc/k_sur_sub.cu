@@ -137,6 +137,13 @@ struct __align__(16) VStage {
 };
 static_assert(offsetof(VStage, li) % 16 == 0 && offsetof(VStage, vb) % 16 == 0 && sizeof(VStage) % 16 == 0,
               "bulk copies need 16-byte aligned destinations");
+// The rows-only stage of the same pipeline (no V box).
+struct __align__(16) RStage {
+    SubStage rows;
+    int32_t hdr[8];
+};
+template <bool BOX> struct StageOf { using T = VStage; };
+template <> struct StageOf<false> { using T = RStage; };
 
 struct VHdr {
     int32_t ok, zlo, xlo, ylo, bx, by, bz;
@@ -148,85 +155,139 @@ __device__ __forceinline__ VHdr vhdr_load(const int32_t *h)
     return VHdr{a.x, a.y, a.z, a.w, b.x, b.y, b.z};
 }
 
-// Thread 0: the rows, box indices and (when the box fits) the V box of tile
-// k0 / kSubTile into one stage, completing on bar.  The box's columns are
-// z-segments [zlo, zlo + bz) of the dense grid, each copied whole: nz, zlo
-// and bz are multiples of 4, so every source and destination is 16-byte
-// aligned and every size a multiple of 16 bytes; the host builder keeps every
-// segment inside its column (zlo + bz <= nz) and every column inside the grid.
-__device__ __forceinline__ void vbox_issue(VStage &st, uint64_t *bar, const GridDev<float> &gd, const float *V,
-                                           int64_t k0, bool det, const VHdr &h)
+// The producer warp's share of the copies of tile k0 / kSubTile into one
+// stage: lane 0 first writes the header and arms the stage's mbarrier with
+// the byte count, then the lanes issue the copies in parallel -- the 7 row
+// copies (rate, index, tensor, divergence, control, detector flag, box
+// index) and, when the box fits, one per box column.  A box column is the
+// z-segment [zlo, zlo + bz) of grid column (xlo + i, ylo + j), copied whole:
+// nz, zlo and bz are multiples of 4, so every source and destination is
+// 16-byte aligned and every size a multiple of 16 bytes; the host builder
+// keeps every segment inside its column and every column inside the grid.
+template <bool BOX>
+__device__ __forceinline__ void vbox_issue(typename StageOf<BOX>::T &st, uint64_t *bar, const GridDev<float> &gd,
+                                           const float *V, int64_t k0, bool det, const VHdr &h, int lane, int64_t ny,
+                                           int64_t nz)
 {
     constexpr uint32_t n = kSubTile;
-    const uint32_t box = h.ok ? (uint32_t)(h.bx * h.by * h.bz) * 4u : 0u;
-    tc::mbar_expect_tx(bar, n * (4 + 4 + 12 + 8 + 1) + (det ? n : 0) + n * 4 + box);
-    tc::bulk_g2s(st.rows.rate, gd.srate + k0, n * 4, bar);
-    tc::bulk_g2s(st.rows.gidx, gd.gidx + k0, n * 4, bar);
-    tc::bulk_g2s(st.rows.d6, gd.d6h + 3 * k0, n * 12, bar);
-    tc::bulk_g2s(st.rows.b3, gd.b3h + 2 * k0, n * 8, bar);
-    tc::bulk_g2s(st.rows.ctl, gd.ctl + k0, n, bar);
-    if (det) tc::bulk_g2s(st.rows.flag, gd.sdflag + k0, n, bar);
-    tc::bulk_g2s(st.li, gd.vli + k0, n * 4, bar);
-    if (h.ok) {
-        const int64_t ny = gd.sx / gd.sy, nz = gd.sy;
-        for (int i = 0; i < h.bx; ++i)
-            for (int j = 0; j < h.by; ++j)
-                tc::bulk_g2s(st.vb + (i * h.by + j) * h.bz, V + ((int64_t)(h.xlo + i) * ny + (h.ylo + j)) * nz + h.zlo,
-                             (uint32_t)h.bz * 4u, bar);
+    const int ncol = (BOX && h.ok) ? h.bx * h.by : 0;
+    if (lane == 0) {
+        st.hdr[0] = BOX ? h.ok : 0;
+        st.hdr[1] = h.by * h.bz;
+        st.hdr[2] = h.bz;
+        const uint32_t box = (uint32_t)ncol * (uint32_t)h.bz * 4u;
+        tc::mbar_expect_tx(bar, n * (4 + 4 + 12 + 8 + 1) + (det ? n : 0) + (BOX ? n * 4 : 0) + box);
     }
-    st.hdr[0] = h.ok;
-    st.hdr[1] = h.by * h.bz;
-    st.hdr[2] = h.bz;
+    __syncwarp();
+    for (int c = lane; c < (BOX ? 7 : 6) + ncol; c += 32) {
+        switch (c) {
+        case 0: tc::bulk_g2s(st.rows.rate, gd.srate + k0, n * 4, bar); break;
+        case 1: tc::bulk_g2s(st.rows.gidx, gd.gidx + k0, n * 4, bar); break;
+        case 2: tc::bulk_g2s(st.rows.d6, gd.d6h + 3 * k0, n * 12, bar); break;
+        case 3: tc::bulk_g2s(st.rows.b3, gd.b3h + 2 * k0, n * 8, bar); break;
+        case 4: tc::bulk_g2s(st.rows.ctl, gd.ctl + k0, n, bar); break;
+        case 5: if (det) tc::bulk_g2s(st.rows.flag, gd.sdflag + k0, n, bar); break;
+        default:
+            if constexpr (BOX) {
+                if (c == 6) {
+                    tc::bulk_g2s(st.li, gd.vli + k0, n * 4, bar);
+                } else {
+                    const int col = c - 7, i = col / h.by, j = col - i * h.by;
+                    tc::bulk_g2s(st.vb + col * h.bz, V + ((int64_t)(h.xlo + i) * ny + (h.ylo + j)) * nz + h.zlo,
+                                 (uint32_t)h.bz * 4u, bar);
+                }
+            }
+        }
+    }
+}
+
+// Named barrier over the 256 consumer threads (id 1) that also returns
+// whether every one of them passed `v` != 0.
+__device__ __forceinline__ int consumers_and(int v)
+{
+    int r;
+    asm volatile(
+        "{\n.reg .pred p, q;\nsetp.ne.s32 p, %1, 0;\nbar.red.and.pred q, 1, %2, p;\nselp.s32 %0, 1, 0, q;\n}\n"
+        : "=r"(r)
+        : "r"(v), "n"(kSubTile)
+        : "memory");
+    return r;
 }
 
 }  // namespace
 
-// 3D V-only substep with the V halo staged: persistent CTAs, two stages; each
-// stage holds a tile's streamed rows and the box of the dense V grid its
-// stencils reach, brought by bulk asynchronous copies issued two tiles ahead,
-// so the threads read the 19-point stencil from shared memory.  A tile whose
-// box exceeds the stage reads V from the grid.  Arithmetic identical to
-// k_sur_substep.  Waits and their failure path as in k_sur_substep_tile.
-template <int MINB>
-__global__ void __launch_bounds__(kSubTile, MINB) k_sur_substep_vbox(GridDev<float> gd, float dt, int cur)
+// 3D V-only substep with the V halo staged.  Persistent CTAs of 8 consumer
+// warps (one voxel per thread of a 256-voxel tile) and one producer warp, two
+// stages: each stage holds a tile's streamed rows and the box of the dense V
+// grid its stencils reach.  The producer fills a stage as soon as the
+// consumers release it (mbarrier `empty`) and arms `full` with the stage's
+// byte count; the consumers wait on `full`, read the 19-point stencil from
+// shared memory and release the stage -- no CTA-wide barrier per tile.  A
+// tile whose box exceeds the stage reads V from the grid.  Arithmetic
+// identical to k_sur_substep.  Every wait is bounded: a consumer wait that
+// runs out sets bit 1 of *serr and ends the consumers' loop; a producer wait
+// that runs out stops the issuing; before leaving, the producer waits
+// (bounded) until the copies it issued have landed.  With BOX false the
+// stages hold the rows only and V comes from the grid (2D and 3D).
+template <int DIM, int MINB, bool BOX>
+__global__ void __launch_bounds__(kSubTile + 32, MINB) k_sur_substep_vbox(GridDev<float> gd, float dt, int cur)
 {
+    using Stage = typename StageOf<BOX>::T;
     extern __shared__ __align__(128) uint8_t vsm[];
-    VStage *stg = reinterpret_cast<VStage *>(vsm);
-    __shared__ __align__(8) uint64_t bar[2];
+    Stage *stg = reinterpret_cast<Stage *>(vsm);
+    __shared__ __align__(8) uint64_t full[2], empty[2];
     const int t = threadIdx.x;
     const int64_t ntiles = (gd.ntissue + kSubTile - 1) / kSubTile;
     const int64_t stride = gridDim.x;
-    int64_t tile = blockIdx.x;
-    if (tile >= ntiles) return;
+    const int64_t tile0 = blockIdx.x;
+    if (tile0 >= ntiles) return;
     const bool det = gd.det != nullptr;
     const uint32_t lim = gd.sub_wait_limit ? gd.sub_wait_limit : kSubWaitLimit;
     const float *__restrict__ V = gd.vg[cur];
-    float *__restrict__ Vn = gd.vg[cur ^ 1];
-    VHdr hnext{};       // thread 0: header of the tile two ahead
     if (t == 0) {
-        tc::mbar_init(&bar[0], 1);
-        tc::mbar_init(&bar[1], 1);
+        tc::mbar_init(&full[0], 1);
+        tc::mbar_init(&full[1], 1);
+        tc::mbar_init(&empty[0], kSubTile / 32);
+        tc::mbar_init(&empty[1], kSubTile / 32);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        if (!gd.sub_skip_copy) vbox_issue(stg[0], &bar[0], gd, V, tile * kSubTile, det, vhdr_load(gd.vbox_hdr + 8 * tile));
-        if (tile + stride < ntiles)
-            vbox_issue(stg[1], &bar[1], gd, V, (tile + stride) * kSubTile, det,
-                       vhdr_load(gd.vbox_hdr + 8 * (tile + stride)));
     }
     __syncthreads();
-    const Clock ck = *gd.clk;
-    for (uint32_t it = 0; tile < ntiles; tile += stride, ++it) {
-        const int s = it & 1;
-        if (t == 0 && tile + 2 * stride < ntiles) hnext = vhdr_load(gd.vbox_hdr + 8 * (tile + 2 * stride));
-        const bool ok = tc::mbar_wait(&bar[s], (it >> 1) & 1, lim);
-        if (!__syncthreads_and(ok ? 1 : 0)) {
-            if (t == 0) {
-                atomicOr(gd.serr, 2);
-                if (it > 0 || !gd.sub_skip_copy) tc::mbar_wait(&bar[s], (it >> 1) & 1, kSubWaitLimit);
-                if (tile + stride < ntiles) tc::mbar_wait(&bar[s ^ 1], ((it + 1) >> 1) & 1, kSubWaitLimit);
+    if (t >= kSubTile) {
+        // ---- producer warp ----
+        const int lane = t - kSubTile;
+        const int64_t ny = BOX ? gd.sx / gd.sy : 0, nz = BOX ? gd.sy : 0;
+        const bool skip0 = gd.sub_skip_copy != 0;   // failure-path test: tile 0's stage is never filled
+        uint32_t issued = 0;
+        for (int64_t tile = tile0; tile < ntiles; tile += stride, ++issued) {
+            const int s = issued & 1;
+            // the whole warp takes one decision (vbox_issue synchronises the warp)
+            const bool free = issued < 2 || tc::mbar_wait(&empty[s], ((issued - 2) >> 1) & 1, lim);
+            if (!__all_sync(0xffffffffu, free)) {
+                if (lane == 0) atomicOr(gd.serr, 2);
+                break;
             }
-            return;
+            if (issued == 0 && skip0) continue;
+            tc::fence_proxy_async();
+            const VHdr h = BOX ? vhdr_load(gd.vbox_hdr + 8 * tile) : VHdr{};
+            vbox_issue<BOX>(stg[s], &full[s], gd, V, tile * kSubTile, det, h, lane, ny, nz);
         }
-        const VStage &st = stg[s];
+        // the copies of the last two stages have landed before the CTA ends
+        for (uint32_t j = issued > 2 ? issued - 2 : 0; j < issued; ++j)
+            if (j > 0 || !skip0) tc::mbar_wait(&full[j & 1], (j >> 1) & 1, kSubWaitLimit);
+        return;
+    }
+    // ---- consumer warps ----
+    float *__restrict__ Vn = gd.vg[cur ^ 1];
+    const Clock ck = *gd.clk;
+    uint32_t it = 0;
+    for (int64_t tile = tile0; tile < ntiles; tile += stride, ++it) {
+        const int s = it & 1;
+        const bool ok = tc::mbar_wait(&full[s], (it >> 1) & 1, lim);
+        if (!consumers_and(ok ? 1 : 0)) {
+            if (t == 0) atomicOr(gd.serr, 2);
+            break;
+        }
+        const Stage &st = stg[s];
         const SubStage &sg = st.rows;
         const int64_t k = tile * kSubTile + t;
         const float r = sg.rate[t];
@@ -238,15 +299,20 @@ __global__ void __launch_bounds__(kSubTile, MINB) k_sur_substep_vbox(GridDev<flo
 #pragma unroll
             for (int i = 0; i < 2; ++i) q[3 + i] = __half22float2(sg.b3[2 * t + i]);
             float Dt[6], Bt[3];
-            sub_tensor_unpack<3>(q, Dt, Bt);
+            sub_tensor_unpack<DIM>(q, Dt, Bt);
             float vc, du;
-            if (st.hdr[0]) {
-                const int64_t li = st.li[t];
-                vc = st.vb[li];
-                du = sub_du_at<3>(gd, st.vb, li, st.hdr[1], st.hdr[2], vc, Dt, Bt);
-            } else {
+            bool staged = false;
+            if constexpr (BOX) {
+                if (st.hdr[0]) {
+                    const int64_t li = st.li[t];
+                    vc = st.vb[li];
+                    du = sub_du_at<DIM>(gd, st.vb, li, st.hdr[1], st.hdr[2], vc, Dt, Bt);
+                    staged = true;
+                }
+            }
+            if (!staged) {
                 vc = V[g];
-                du = sub_du_at<3>(gd, V, g, gd.sx, gd.sy, vc, Dt, Bt);
+                du = sub_du_at<DIM>(gd, V, g, gd.sx, gd.sy, vc, Dt, Bt);
             }
             const float ist = grid_stim(gd, ck, sg.ctl[t], k);
             const float dvdt = r - ist;
@@ -256,11 +322,8 @@ __global__ void __launch_bounds__(kSubTile, MINB) k_sur_substep_vbox(GridDev<flo
             const bool bad = !(vn == vn) || vn < gd.vmin_ok || vn > gd.vmax_ok;
             if (bad) atomicAdd(gd.nbad, 1ull);
         }
-        __syncthreads();   // every thread is done with stage s
-        if (t == 0 && tile + 2 * stride < ntiles) {
-            tc::fence_proxy_async();
-            vbox_issue(stg[s], &bar[s], gd, V, (tile + 2 * stride) * kSubTile, det, hnext);
-        }
+        __syncwarp();
+        if ((t & 31) == 0) tc::mbar_arrive(&empty[s]);   // this warp is done with stage s
     }
 }
 
@@ -301,19 +364,20 @@ template <int DIM, int MINB> cudaError_t launch_tile(const GridDev<float> &gd, d
     return cudaGetLastError();
 }
 
-template <int MINB> cudaError_t launch_vbox(const GridDev<float> &gd, double dt, int cur, cudaStream_t st)
+template <int DIM, int MINB, bool BOX>
+cudaError_t launch_vbox(const GridDev<float> &gd, double dt, int cur, cudaStream_t st)
 {
     static std::atomic<uint64_t> done{0}, carve{0};
-    const uint32_t bytes = 2 * sizeof(VStage);
-    cudaError_t e = tc::smem_attr_once(k_sur_substep_vbox<MINB>, bytes, done);
-    if (e == cudaSuccess) e = carveout_once(k_sur_substep_vbox<MINB>, carve);
+    const uint32_t bytes = 2 * sizeof(typename StageOf<BOX>::T);
+    cudaError_t e = tc::smem_attr_once(k_sur_substep_vbox<DIM, MINB, BOX>, bytes, done);
+    if (e == cudaSuccess) e = carveout_once(k_sur_substep_vbox<DIM, MINB, BOX>, carve);
     if (e != cudaSuccess) return e;
     int dev = 0, nsm = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const int64_t ntiles = (gd.ntissue + kSubTile - 1) / kSubTile;
     const int64_t grid = ntiles < (int64_t)nsm * MINB ? ntiles : (int64_t)nsm * MINB;
-    k_sur_substep_vbox<MINB><<<(unsigned)grid, kSubTile, bytes, st>>>(gd, (float)dt, cur);
+    k_sur_substep_vbox<DIM, MINB, BOX><<<(unsigned)grid, kSubTile + 32, bytes, st>>>(gd, (float)dt, cur);
     return cudaGetLastError();
 }
 
@@ -324,11 +388,24 @@ bool al16(const void *p) { return p && ((uintptr_t)p & 15u) == 0; }
 cudaError_t launch_sur_substep(const GridDev<float> &gd, double dt, int cur, int dim, int variant, cudaStream_t st)
 {
     if (gd.ntissue <= 0) return cudaSuccess;
-    if (variant >= 200) {
-        if (dim == 3 && gd.d6 && gd.vbox_hdr && gd.vli && al16(gd.vli) && al16(gd.d6h) && al16(gd.b3h) &&
-            al16(gd.srate) && al16(gd.gidx) && al16(gd.ctl) && al16(gd.vg[0]) && al16(gd.vg[1]) && gd.serr &&
-            (!gd.det || al16(gd.sdflag)))
-            return variant == 203 ? launch_vbox<3>(gd, dt, cur, st) : launch_vbox<4>(gd, dt, cur, st);
+    const bool rows_ok = dim >= 2 && gd.d6 && al16(gd.d6h) && al16(gd.b3h) && al16(gd.srate) && al16(gd.gidx) &&
+                         al16(gd.ctl) && gd.serr && (!gd.det || al16(gd.sdflag));
+    if (variant >= 300) {
+        // rows staged by a producer warp, V from the grid (2D/3D)
+        if (rows_ok) {
+            if (dim == 2) {
+                if (variant == 306) return launch_vbox<2, 6, false>(gd, dt, cur, st);
+                if (variant == 305) return launch_vbox<2, 5, false>(gd, dt, cur, st);
+                return launch_vbox<2, 4, false>(gd, dt, cur, st);
+            }
+            if (variant == 306) return launch_vbox<3, 6, false>(gd, dt, cur, st);
+            if (variant == 305) return launch_vbox<3, 5, false>(gd, dt, cur, st);
+            return launch_vbox<3, 4, false>(gd, dt, cur, st);
+        }
+        variant = 105;
+    } else if (variant >= 200) {
+        if (dim == 3 && rows_ok && gd.vbox_hdr && gd.vli && al16(gd.vli) && al16(gd.vg[0]) && al16(gd.vg[1]))
+            return variant == 203 ? launch_vbox<3, 3, true>(gd, dt, cur, st) : launch_vbox<3, 4, true>(gd, dt, cur, st);
         variant = 105;
     }
     const bool tile = variant >= 100;

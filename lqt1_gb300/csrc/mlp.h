@@ -48,7 +48,12 @@ struct GemmArgs {
     const float *Z;              // kEpiDact: pre-activation [M][N]
     int ksplit;                  // kEpiAtomic: split K over grid.z
     int *err;                    // set to 2 if a tensor-core completion wait ran out (or NULL)
+    float *partial;              // kEpiAtomic with ksplit > 1: [slices][M][N] workspace; the slices
+                                 // are then added into C in slice order (same bits every run);
+                                 // NULL = float atomics into C (order-dependent last bits)
 };
+// Slices of a split-K GEMM and the workspace floats it needs (0 without a split).
+int gemm_splitk_slices(int K, int ksplit);
 cudaError_t launch_gemm_bf16(const GemmArgs &g, cudaStream_t st);
 
 }  // namespace lqt

@@ -54,8 +54,8 @@ cudaError_t launch_sur_grid(const GridDev<float> &gd, const SurGrid &sg, int cur
 uint32_t sur_grid_smem_bytes();
 
 cudaError_t launch_sur_datagen(const SurCell *cells, int64_t ncells, const ModelK *models, const StepK &k,
-                               const StepK &kmac, float *X, float *D, unsigned long long *counter, int64_t cap,
-                               uint64_t seed, float dvdt_max, float prob, float jitter, int nsub,
+                               const StepK &kmac, float *X, float *D, int64_t *counts, const int64_t *offsets,
+                               int64_t cap, uint64_t seed, float dvdt_max, float prob, float jitter, int nsub,
                                cudaStream_t st);
 cudaError_t launch_sur_prepare(const float *X, const float *D, const int64_t *idx, int64_t n, const float *norm,
                                __nv_bfloat16 *xb, float *t, cudaStream_t st);

@@ -133,13 +133,14 @@ class Sim:
 
     def substep_variant(self, variant: int = -1, timings: bool = False):
         """Force the V-only substep's kernel variant (5, 6, 8 direct; 105, 106,
-        108 staged by bulk copies; 203, 204 with the V halo staged too) or,
+        108 staged by bulk copies; 203, 204 with the V halo staged too; 304,
+        305, 306 rows streamed by a producer warp) or,
         with -1, report the current one; with timings, also the last
         autotune's ms per variant (same order)."""
         L = N.lib()
         L.lqt_sim_substep_variant.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.c_void_p]
         ch = C.c_int32()
-        ms = np.zeros(8, np.float32)
+        ms = np.zeros(11, np.float32)
         N.check(L.lqt_sim_substep_variant(self._h, int(variant), C.byref(ch), _p(ms)), "lqt_sim_substep_variant")
         return (ch.value, ms) if timings else ch.value
 

@@ -272,8 +272,9 @@ def test_speed_gain_over_plain_step(lq, torch, net):
 @pytest.mark.parametrize("dim", [2, 3])
 def test_substep_variants_bit_identical(lq, net, dim):
     """Every kernel of the V-only substep (direct loads at 5 and 8 CTAs/SM;
-    tiles staged in shared memory by bulk copies at 5, 6 and 8 CTAs/SM; in 3D
-    also the tiles' V halo boxes staged, at 3 and 4 CTAs/SM) gives the same
+    tiles staged in shared memory by bulk copies at 5, 6 and 8 CTAs/SM; the
+    tiles' rows streamed by a producer warp at 4, 5 and 6 CTAs/SM; in 3D also
+    the tiles' V halo boxes staged, at 3 and 4 CTAs/SM) gives the same
     bits: state, V, detector and surrogate counters after the upstroke and
     into the plateau of an anisotropic grid whose voxel count is not a
     multiple of the 256-voxel tile (3D: nz = 52, a multiple of 4, so the V
@@ -290,7 +291,7 @@ def test_substep_variants_bit_identical(lq, net, dim):
         types, fibre, mask, dx = v.types, v.fibre, v.s1_mask, 0.2
     m = lq.model("baseline", gks_scale=0.5, pca_scale=1.5, gks_iso_scale=1.2)
     out = {}
-    for var in (5, 8, 105, 106, 108) + ((203, 204) if dim == 3 else ()):
+    for var in (5, 8, 105, 106, 108, 304, 305, 306) + ((203, 204) if dim == 3 else ()):
         sim = lq.Sim(types, dx, fibre=fibre, precision=lq.MIXED, model=m)
         assert sim.n % 256 != 0
         sim.set_protocol(bcl=1000.0, s1_mask=mask, s1_start=0.0, s1_duration=2.0, s1_strength=-52.0)
@@ -356,12 +357,15 @@ def test_macro_length_and_rejection_counters(lq, orc, net):
     plain.close()
 
 
-def test_substep_wait_timeout_is_reported_and_recoverable(lq, net):
+@pytest.mark.parametrize("variant", [105, 304])
+def test_substep_wait_timeout_is_reported_and_recoverable(lq, net, variant):
     """Failure path of the staged substep's bounded waits, without a GPU
     fault: a test setting leaves the first tile's copies of every CTA out, so
     nothing completes that mbarrier phase and the wait runs out after a short
-    bound.  The kernel sets the error bit and returns; surrogate_stats reports
-    it, lqt_sim_check raises, and with the setting cleared the same
+    bound (105: all threads wait on the copies; 304: the consumer warps wait
+    on the stage, then the producer warp on the stage the consumers never
+    release).  The kernel sets the error bit and returns; surrogate_stats
+    reports it, lqt_sim_check raises, and with the setting cleared the same
     simulation steps on normally."""
     v = lq.geometry.ventricle(nx=44, ny=44, nz=50, dx=0.2, a_out=4.0, c_out=8.0, wall=2.0, z_base=9.0,
                               island_radius=1.5, stim_radius=1.2)
@@ -370,7 +374,7 @@ def test_substep_wait_timeout_is_reported_and_recoverable(lq, net):
     sim.set_protocol(bcl=800.0, s1_mask=v.s1_mask, s1_start=0.0, s1_duration=2.0, s1_strength=-52.0)
     sim.set_surrogate(net)
     sim.tune(4)
-    assert sim.substep_variant(105) == 105
+    assert sim.substep_variant(variant) == variant
     sim.step(2 * net.nsub)
     assert sim.surrogate_stats()["wait_timeouts"] == 0 and sim.check() == 0
     sim.set_wait_test(True, 256)
