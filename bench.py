@@ -249,6 +249,8 @@ def main():
                          "203/204 staged rows and V halo, 304/305/306 rows from a producer warp; -1 = autotune)")
     ap.add_argument("--sur-dvdt-max", type=float, default=1.5, help="surrogate eligibility: |dV/dt| bound, mV/ms")
     ap.add_argument("--sur-vstep-max", type=float, default=0.4, help="surrogate residual check: ionic dV per macro step")
+    ap.add_argument("--sur-foot-dvdt", type=float, default=0.1,
+                    help="surrogate wave-foot gate: no macro step where V < -40 mV rises faster than this (0 = off)")
     ap.add_argument("--fp64-steps", type=int, default=10)
     ap.add_argument("--mixed-steps", type=int, default=-1, help="steps of the plain mixed leg (-1 = --steps)")
     ap.add_argument("--no-accuracy", dest="accuracy", action="store_false")
@@ -300,7 +302,8 @@ def main():
     w = build_workload(args.workload)
     stream = torch.cuda.Stream()
     net = S.load(args.weights, stream=stream.cuda_stream)
-    SUR_CFG.update(dvdt_max=args.sur_dvdt_max, vstep_max=args.sur_vstep_max)
+    SUR_CFG.update(dvdt_max=args.sur_dvdt_max, vstep_max=args.sur_vstep_max, foot_dvdt=args.sur_foot_dvdt,
+                   foot_v=-40.0)
     beat = int(round(w["bcl"] / 0.02))
     phase_mode = args.steps < beat
     phases = PHASES if phase_mode else (("beat", None),)
@@ -473,7 +476,7 @@ def main():
             v5 = world * n * args.steps * len(phases) / (ms5 / 1e3)
             at_spec = {"value": v5, "unit": UNIT, "windows": per5,
                        "form": "0.1 ms macro steps (network trained for nsub = 5), |dV/dt| <= 1 mV/ms, "
-                               "ionic dV <= 0.3 mV per macro step",
+                               "ionic dV <= 0.3 mV per macro step, wave-foot gate as the headline's",
                        "accepted_frac_of_voxel_macro_steps": st5["accepted"] / max(1, st5["macro_steps"] * n),
                        "over_fp64": None if fp64 is None else v5 / fp64["value"],
                        "blowup_voxel_steps": s5.check(), "network": {k: net5.meta.get(k) for k in
@@ -543,8 +546,9 @@ def main():
             "config": {"workload": w["desc"], "tissue_voxels": n,
                        "form": "FP32 + learned surrogate (FP32 gates/currents/diffusion, Kahan-compensated FP32 "
                                "concentrations; %g ms macro steps of a coarse TPORd step + BF16 tcgen05 MLP "
-                               "correction where |dV/dt| <= %g mV/ms, plain 0.02 ms steps elsewhere)"
-                               % (round(0.02 * net.nsub, 3), args.sur_dvdt_max),
+                               "correction where |dV/dt| <= %g mV/ms and not at a wave's foot (V < -40 mV rising "
+                               "faster than %g mV/ms), plain 0.02 ms steps elsewhere)"
+                               % (round(0.02 * net.nsub, 3), args.sur_dvdt_max, args.sur_foot_dvdt),
                        "surrogate_thresholds": dict(SUR_CFG),
                        "deviations_from_stated_config5": {
                            "macro_step_ms": [round(0.02 * net.nsub, 3), 0.1],

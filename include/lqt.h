@@ -581,7 +581,8 @@ int lqt_sur_prepare(lqt_mlp *m, const float *x_dev, const float *d_dev,
 /* The surrogate inside a tissue simulation (mixed form only).  Every nsub
  * steps (steps whose index is a multiple of nsub; nsub divides 50, 0 = 5)
  * one kernel offers each tissue voxel whose |dV/dt| over the last step is at
- * most dvdt_max, and that no stimulus reaches in the next nsub steps, to the
+ * most dvdt_max, that is not at the foot of a wave (foot_dvdt, foot_v), and
+ * that no stimulus reaches in the next nsub steps, to the
  * surrogate: one coarse TPORd step of nsub * dt plus the network's
  * correction (use_net = 1; 0 = the coarse step alone).  The residual check (every normalised correction within
  * +-kappa times its bound, lqt_mlp_set_bounds; gates within [0, 1];
@@ -601,6 +602,13 @@ typedef struct lqt_sur_config {
     double vstep_max;   /* mV per macro step, e.g. 0.4 */
     int32_t use_net;
     int32_t nsub;       /* plain steps per macro step; divides 50; 0 = 5 */
+    /* wave-foot gate: a voxel below foot_v (mV) whose V rose faster than
+     * foot_dvdt (mV/ms) over the last step is not offered -- the foot of an
+     * approaching wave, where diffusion drives V towards threshold and an
+     * ionic state advanced without it would delay the upstroke.  foot_dvdt
+     * = 0 turns the gate off (then |dV/dt| <= dvdt_max alone decides). */
+    double foot_dvdt;   /* mV/ms, e.g. 0.1 (the Python default) */
+    double foot_v;      /* mV, e.g. -40 */
 } lqt_sur_config;
 int lqt_sim_set_surrogate(lqt_sim *s, lqt_mlp *m, const lqt_sur_config *cfg);
 /* Counters since the last reset: macro steps launched, voxel offers, voxels

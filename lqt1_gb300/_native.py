@@ -69,7 +69,7 @@ _lib = None
 
 class SurConfig(C.Structure):
     _fields_ = [("dvdt_max", C.c_double), ("kappa", C.c_double), ("vstep_max", C.c_double), ("use_net", C.c_int32),
-                ("nsub", C.c_int32)]
+                ("nsub", C.c_int32), ("foot_dvdt", C.c_double), ("foot_v", C.c_double)]
 
 
 def lib():

@@ -314,6 +314,8 @@ int launch_sur_if_due(lqt_sim *s)
     sg.par[1] = (float)s->p.model.pca_scale;
     sg.par[2] = (float)s->p.model.gks_iso_scale;
     sg.dvdt_max = (float)s->sur_cfg.dvdt_max;
+    sg.foot_dvdt = s->sur_cfg.foot_dvdt > 0 ? (float)s->sur_cfg.foot_dvdt : INFINITY;
+    sg.foot_v = (float)s->sur_cfg.foot_v;
     sg.kappa = (float)s->sur_cfg.kappa;
     sg.vstep_max = (float)s->sur_cfg.vstep_max;
     sg.nsub = s->sur_nsub;
@@ -1229,9 +1231,10 @@ int lqt_sim_set_surrogate(lqt_sim *s, lqt_mlp *m, const lqt_sur_config *cfg)
         return fail(LQT_ERR_INVALID, "lqt_sim_set_surrogate: the network's inputs carry the GKs, PCa and GKs-ISO "
                                      "factors only; models with ISO gate shifts or SUPREP are not covered");
     if (!cfg || !(cfg->dvdt_max > 0) || !(cfg->kappa > 0) || !(cfg->vstep_max > 0) ||
-        !sur_nsub_ok(sur_nsub_or_default(cfg->nsub)) || (cfg->use_net != 0 && cfg->use_net != 1))
+        !sur_nsub_ok(sur_nsub_or_default(cfg->nsub)) || (cfg->use_net != 0 && cfg->use_net != 1) ||
+        !(cfg->foot_dvdt >= 0) || !std::isfinite(cfg->foot_v))
         return fail(LQT_ERR_INVALID, "lqt_sim_set_surrogate: dvdt_max, kappa, vstep_max > 0; use_net 0/1; "
-                                     "nsub divides 50 (0 = 5)");
+                                     "nsub divides 50 (0 = 5); foot_dvdt >= 0; foot_v finite");
     MlpDev w;
     const float *nrm = nullptr;
     if (!mlp_device_view(m, &w, &nrm)) return fail(LQT_ERR_INVALID, "lqt_sim_set_surrogate: network not initialised");

@@ -112,15 +112,26 @@ __device__ __forceinline__ void grid_detect(const GridDev<R> &gd, const Clock &c
     grid_detect_rec(gd, ck, k, gd.det[k], vc, vn, dvdt);
 }
 
+// Is the S1 stimulus of a voxel with this onset on at within-cycle time tb?
+// Per-voxel onset within each cycle, compared in FP64 as GPU3D.cu:397-409
+// does.  Out of line on purpose: inlined, the compiler evaluates these FP64
+// operations under a predicate for every voxel of the kernels that never use
+// onsets, and GB300's FP64 pipe is slow enough for five of them per warp to
+// keep it half busy in the V-only substep.
+static __device__ __noinline__ bool onset_s1_on(double tb, double s1_start, double s1_dur, float onset)
+{
+    const double on = s1_start + (double)onset;
+    return tb >= on && tb < on + s1_dur;
+}
+
 // Stimulus current of voxel k at the clock's step.
 template <typename R>
 __device__ __forceinline__ R grid_stim(const GridDev<R> &gd, const Clock &ck, uint8_t ctl, int64_t k)
 {
     R ist = 0;
     if (gd.onset) {
-        // per-voxel onset within each cycle (GPU3D.cu:397-409)
-        const double on = gd.s1_start + (double)gd.onset[k];
-        if ((ctl & kCtlS1) && ck.s1_cycle_ok && ck.tb >= on && ck.tb < on + gd.s1_dur) ist = gd.s1_strength;
+        if ((ctl & kCtlS1) && ck.s1_cycle_ok && onset_s1_on(ck.tb, gd.s1_start, gd.s1_dur, gd.onset[k]))
+            ist = gd.s1_strength;
     } else if (ck.s1_on && (ctl & kCtlS1)) {
         ist = gd.s1_strength;
     }

@@ -208,6 +208,16 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v)
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Per-voxel onsets: could the S1 stimulus of a voxel with this onset start
+// within the next nsub + 1 steps (this cycle's or the next's)?  FP64, out of
+// line for the reason given at onset_s1_on.
+__device__ __noinline__ bool onset_s1_ahead(const GridDev<float> &gd, double tb, int nsub, float onset)
+{
+    const double on = gd.s1_start + (double)onset;
+    const double span = (nsub + 1) * gd.dt;
+    return (tb + span >= on && tb <= on + gd.s1_dur) || (tb - gd.bcl + span >= on);
+}
+
 // Does any stimulus reach voxel k during steps [ck.step, ck.step + nsub)?
 // Window schedule: the current window (first with off > step) is the only
 // candidate.  Per-voxel onsets: a conservative test on the within-cycle time.
@@ -217,12 +227,7 @@ __device__ __forceinline__ bool stim_ahead(const GridDev<float> &gd, const Clock
     const int64_t s0 = ck.step, s1 = ck.step + nsub;
     if ((ctl & kCtlS2) && gd.s2_win.on < s1 && gd.s2_win.off > s0) return true;
     if (!(ctl & kCtlS1)) return false;
-    if (gd.onset) {
-        const double on = gd.s1_start + (double)gd.onset[k];
-        const double span = (nsub + 1) * gd.dt;
-        const double tb = ck.tb;
-        return (tb + span >= on && tb <= on + gd.s1_dur) || (tb - gd.bcl + span >= on);
-    }
+    if (gd.onset) return onset_s1_ahead(gd, ck.tb, nsub, gd.onset[k]);
     const int32_t nwin = gd.win ? gd.nwin : 0;
     const int32_t w = ck.widx < 0 ? 0 : ck.widx;
     return w < nwin && gd.win[w].on < s1 && gd.win[w].off > s0;
@@ -300,7 +305,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
         bool elig = false, need_det = false;
         float vc = 0.f;
         int ct = 0;
+        // 1. the state, loaded once (its loads need only k, so they are in
+        //    flight while the index, V and detector loads resolve): the
+        //    features are built from it and the coarse step advances it in
+        //    registers while the first layer's MMAs run
+        CellState<float> c;
         if (k < nt) {
+            load_cell(c, gd.s, k);
             const int64_t g = dim == 1 ? k : (int64_t)gd.gidx[k];
             vc = V[g];
             const float dv = (vc - Vp[g]) * inv_dt;
@@ -318,16 +329,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
                 need_det = opens || ph == kDetRise || (ph == kDetWait && vc > gd.act_thr - kDetMargin) ||
                            (ph == kDetFall && !(vc < d.y - kDetMargin && vc > d.y - 0.5f * amp + kDetMargin));
             }
-            elig = net_ok && fabsf(dv) <= sg.dvdt_max && !stim_ahead(gd, ck, ctl, k, sg.nsub);
+            // (a NaN dV/dt fails the first test; the foot test keeps a rising
+            // voxel below the foot voltage on the plain step)
+            elig = net_ok && fabsf(dv) <= sg.dvdt_max && !(vc < sg.foot_v && dv > sg.foot_dvdt) &&
+                   !stim_ahead(gd, ck, ctl, k, sg.nsub);
         }
-        // 1. the state, loaded once: the features are built from it and the
-        //    coarse step advances it in registers while the first layer's
-        //    MMAs run
-        CellState<float> c;
-        if (elig) {
-            load_cell(c, gd.s, k);
-            c.v = vc;
-        }
+        c.v = vc;
         if (use_net) {
             // features (the previous tile's MMAs have all completed)
             uint4 *row[kMlpIn / 8];

@@ -45,6 +45,7 @@ struct SurGrid {
     StepT<float> kmac;              // the coarse step (dt = nsub * plain dt)
     float par[3];                   // GKs, PCa and GKs-ISO factors of the model
     float dvdt_max;                 // offer only where |dV/dt| <= dvdt_max (mV/ms)
+    float foot_dvdt, foot_v;        // and not where V < foot_v rises faster than foot_dvdt (0 = off)
     float kappa;                    // multiplier of out_bound in the residual check
     float vstep_max;                // bound on the macro step's ionic V change (mV)
     int nsub;                       // plain steps per macro step

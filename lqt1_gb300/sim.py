@@ -171,18 +171,21 @@ class Sim:
 
     # ---- learned surrogate ---------------------------------------------------------
     def set_surrogate(self, mlp=None, *, dvdt_max: float = 1.5, kappa: float = 1.5, vstep_max: float = 0.4,
-                      use_net: bool = True, nsub: int | None = None):
+                      use_net: bool = True, nsub: int | None = None, foot_dvdt: float = 0.1, foot_v: float = -40.0):
         """Attach a trained surrogate network (lqt1_gb300.surrogate.Mlp) or
         detach (None).  Mixed form only; see lqt_sim_set_surrogate.  The macro
         step is the network's own length (mlp.nsub plain steps) unless nsub
-        overrides it."""
+        overrides it; foot_dvdt > 0 keeps voxels below foot_v whose V rises
+        faster than foot_dvdt (mV/ms) on the plain step (the foot of a wave;
+        0 = off)."""
         L = N.lib()
         L.lqt_sim_set_surrogate.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         if mlp is None:
             N.check(L.lqt_sim_set_surrogate(self._h, None, None), "lqt_sim_set_surrogate")
             self._sur = None
             return
-        cfg = N.SurConfig(dvdt_max, kappa, vstep_max, int(bool(use_net)), int(nsub or getattr(mlp, "nsub", 5)))
+        cfg = N.SurConfig(dvdt_max, kappa, vstep_max, int(bool(use_net)), int(nsub or getattr(mlp, "nsub", 5)),
+                          float(foot_dvdt), float(foot_v))
         N.check(L.lqt_sim_set_surrogate(self._h, mlp._h, C.byref(cfg)), "lqt_sim_set_surrogate")
         self._sur = mlp     # keep the network alive while attached
 
