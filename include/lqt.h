@@ -323,17 +323,22 @@ int lqt_sim_set_state(lqt_sim *s, const double *state_host);
 int lqt_sim_set_electrodes(lqt_sim *s, int32_t n, const double *xyz_host,
                            int32_t every);
 /* V of every tissue voxel into a host buffer without waiting (the reference
- * copies V back every step, GPU3D.cu:1802): the gather into one of two device
+ * copies V back every step, GPU3D.cu:1802): the gather into one of 16 device
  * slots runs on the simulation's stream, the copy on four copy streams, so it
- * overlaps the next steps.  The buffer (pinned memory for a true overlap) is
- * complete after lqt_sim_wait_v; a buffer must not be reused before that. */
+ * overlaps the next steps; the steps wait only when all 16 slots hold copies
+ * still in flight.  The copies of one simulation are numbered 0, 1, ... in
+ * call order (the first call after lqt_sim_create is copy 0) and complete in
+ * that order.  The buffer (pinned memory for a true overlap) is complete after
+ * lqt_sim_wait_v_upto(its number) or lqt_sim_wait_v, and must not be reused
+ * before. */
 int lqt_sim_get_v_async(lqt_sim *s, void *v_host, int as_double);
-/* Waits for every read-back copy in flight.  The GPU idles while the host
- * waits on the newest copy, so a caller that reads V back every step keeps
- * a ring of buffers and waits once per ring (32 buffers: 0.31 ms per step of
- * the 7.1M-voxel surrogate form, against 0.38 ms with a wait every 8 steps
- * and 0.26 ms without read-back). */
+/* Waits for every read-back copy in flight. */
 int lqt_sim_wait_v(lqt_sim *s);
+/* Waits for read-back copies 0..seq (seq < the number of copies issued).  A
+ * caller that reads V back every step keeps a ring of host buffers and waits
+ * for the copy that last filled a buffer before reusing it: the host then
+ * never waits on the newest copy, and the GPU never idles on the host. */
+int lqt_sim_wait_v_upto(lqt_sim *s, int64_t seq);
 
 /* Samples recorded since the electrodes were set: [nsamples][n], and time. */
 int lqt_sim_get_ecg(lqt_sim *s, int64_t max_samples, double *phi_host,

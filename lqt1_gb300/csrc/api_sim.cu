@@ -97,14 +97,16 @@ struct lqt_sim {
     unsigned long long *sur_stats = nullptr;
     int *sur_err = nullptr;
     int64_t sur_launches = 0;
-    // asynchronous V read-back: two device slots, a copy stream, events
-    // asynchronous V read-back: two device slots; each copy is split over
-    // kCopyStreams streams so that several copy engines share the host link
-    static constexpr int kCopyStreams = 4;
-    void *vslot[2] = {nullptr, nullptr};
+    // asynchronous V read-back: a ring of kVSlots device slots, so that the
+    // copies of the short steps between two macro steps can trail behind them
+    // and catch up during the long one; each copy is split over kCopyStreams
+    // streams (several copy engines share the host link) and joined into one
+    // completion event per copy, kept for the last kVDone copies
+    static constexpr int kCopyStreams = 4, kVSlots = 16, kVDone = 64;
+    void *vslot[kVSlots] = {};
     cudaStream_t copy_stream[kCopyStreams] = {};
-    cudaEvent_t gathered[2] = {nullptr, nullptr}, copied[2][kCopyStreams] = {};
-    int vslot_next = 0;
+    cudaEvent_t gathered = nullptr, chunk_done[kCopyStreams] = {}, vdone[kVDone] = {};
+    int64_t v_issued = 0;           // lqt_sim_get_v_async calls so far (the next copy's number)
     // output sampling: tissue mask of the dense grid, lattice buffer
     uint8_t *tmask = nullptr;
     double *samp = nullptr;
@@ -118,11 +120,11 @@ struct lqt_sim {
     {
         for (cudaStream_t c : copy_stream)
             if (c) cudaStreamSynchronize(c);
-        for (int i = 0; i < 2; ++i) {
-            if (gathered[i]) cudaEventDestroy(gathered[i]);
-            for (cudaEvent_t e : copied[i])
-                if (e) cudaEventDestroy(e);
-        }
+        if (gathered) cudaEventDestroy(gathered);
+        for (cudaEvent_t e : chunk_done)
+            if (e) cudaEventDestroy(e);
+        for (cudaEvent_t e : vdone)
+            if (e) cudaEventDestroy(e);
         for (cudaStream_t c : copy_stream)
             if (c) cudaStreamDestroy(c);
         if (graph) cudaGraphExecDestroy(graph);
@@ -319,6 +321,8 @@ int launch_sur_if_due(lqt_sim *s)
     sg.kappa = (float)s->sur_cfg.kappa;
     sg.vstep_max = (float)s->sur_cfg.vstep_max;
     sg.nsub = s->sur_nsub;
+    sg.inv_dt = (float)(1.0 / s->p.dt);
+    sg.inv_mac = (float)(1.0 / (s->sur_nsub * s->p.dt));
     sg.use_net = s->sur_cfg.use_net;
     CK(cudaMemsetAsync(s->plist_n, 0, sizeof(unsigned long long), s->stream));
     CK(launch_sur_grid(devf<float>(s), sg, s->cur, s->dim, s->stream));
@@ -897,24 +901,27 @@ int lqt_sim_get_v_async(lqt_sim *s, void *v_host, int as_double)
     if (!s || !v_host) return fail(LQT_ERR_INVALID, "lqt_sim_get_v_async: NULL");
     const int64_t n = s->ntissue;
     const size_t esz = as_double ? 8 : 4;
-    constexpr int nc = lqt_sim::kCopyStreams;
+    constexpr int nc = lqt_sim::kCopyStreams, ns = lqt_sim::kVSlots, nd = lqt_sim::kVDone;
+    static_assert(nd > ns, "a slot's previous copy must still have its completion event");
     if (!s->copy_stream[0]) {
-        if (s->mem.alloc(&s->vslot[0], n * 8) || s->mem.alloc(&s->vslot[1], n * 8)) return LQT_ERR_NOMEM;
-        for (int c = 0; c < nc; ++c) CK(cudaStreamCreateWithFlags(&s->copy_stream[c], cudaStreamNonBlocking));
-        for (int i = 0; i < 2; ++i) {
-            CK(cudaEventCreateWithFlags(&s->gathered[i], cudaEventDisableTiming));
-            for (int c = 0; c < nc; ++c) {
-                CK(cudaEventCreateWithFlags(&s->copied[i][c], cudaEventDisableTiming));
-                CK(cudaEventRecord(s->copied[i][c], s->copy_stream[c]));
-            }
+        for (int i = 0; i < ns; ++i)
+            if (s->mem.alloc(&s->vslot[i], n * 8)) return LQT_ERR_NOMEM;
+        for (int c = 0; c < nc; ++c) {
+            CK(cudaStreamCreateWithFlags(&s->copy_stream[c], cudaStreamNonBlocking));
+            CK(cudaEventCreateWithFlags(&s->chunk_done[c], cudaEventDisableTiming));
         }
+        CK(cudaEventCreateWithFlags(&s->gathered, cudaEventDisableTiming));
+        for (int i = 0; i < nd; ++i) CK(cudaEventCreateWithFlags(&s->vdone[i], cudaEventDisableTiming));
     }
-    const int k = s->vslot_next;
-    s->vslot_next ^= 1;
-    void *slot = s->vslot[k];
+    const int64_t seq = s->v_issued;
+    void *slot = s->vslot[seq % ns];
+    cudaEvent_t done = s->vdone[seq % nd];
+    // copy seq - nd used this completion event: the host waits for it before
+    // the event is recorded again (so every copy older than the last nd is
+    // known complete), and the gather waits for the slot's previous copy
+    if (seq >= nd) CK(cudaEventSynchronize(done));
+    if (seq >= ns) CK(cudaStreamWaitEvent(s->stream, s->vdone[(seq - ns) % nd], 0));
     const int32_t *gi = s->dim > 1 ? s->gidx : nullptr;
-    // the slot's previous copy must be done before the gather overwrites it
-    for (int c = 0; c < nc; ++c) CK(cudaStreamWaitEvent(s->stream, s->copied[k][c], 0));
     if (s->fp64()) {
         if (as_double) CK((launch_gather_v<double, double>((double *)s->vg[s->cur], gi, (double *)slot, n, s->stream)));
         else CK((launch_gather_v<double, float>((double *)s->vg[s->cur], gi, (float *)slot, n, s->stream)));
@@ -922,18 +929,24 @@ int lqt_sim_get_v_async(lqt_sim *s, void *v_host, int as_double)
         if (as_double) CK((launch_gather_v<float, double>((float *)s->vg[s->cur], gi, (double *)slot, n, s->stream)));
         else CK((launch_gather_v<float, float>((float *)s->vg[s->cur], gi, (float *)slot, n, s->stream)));
     }
-    CK(cudaEventRecord(s->gathered[k], s->stream));
-    // nc chunks of whole 256-byte blocks (the last takes the rest), one per stream
+    CK(cudaEventRecord(s->gathered, s->stream));
+    // nc chunks of whole 256-byte blocks (the last takes the rest), one per
+    // stream, joined on stream 0 into the copy's completion event
     const size_t bytes = (size_t)n * esz;
     const size_t chunk = (bytes / nc + 255) / 256 * 256;
     for (int c = 0; c < nc; ++c) {
         const size_t off = std::min(bytes, c * chunk);
         const size_t len = std::min(bytes, off + chunk) - off;
-        CK(cudaStreamWaitEvent(s->copy_stream[c], s->gathered[k], 0));
+        CK(cudaStreamWaitEvent(s->copy_stream[c], s->gathered, 0));
         if (len) CK(cudaMemcpyAsync((char *)v_host + off, (const char *)slot + off, len, cudaMemcpyDeviceToHost,
                                     s->copy_stream[c]));
-        CK(cudaEventRecord(s->copied[k][c], s->copy_stream[c]));
+        if (c > 0) {
+            CK(cudaEventRecord(s->chunk_done[c], s->copy_stream[c]));
+            CK(cudaStreamWaitEvent(s->copy_stream[0], s->chunk_done[c], 0));
+        }
     }
+    CK(cudaEventRecord(done, s->copy_stream[0]));
+    s->v_issued = seq + 1;
     return LQT_OK;
 }
 
@@ -942,6 +955,18 @@ int lqt_sim_wait_v(lqt_sim *s)
     if (!s) return fail(LQT_ERR_INVALID, "lqt_sim_wait_v: NULL");
     for (cudaStream_t c : s->copy_stream)
         if (c) CK(cudaStreamSynchronize(c));
+    return LQT_OK;
+}
+
+int lqt_sim_wait_v_upto(lqt_sim *s, int64_t seq)
+{
+    if (!s) return fail(LQT_ERR_INVALID, "lqt_sim_wait_v_upto: NULL");
+    if (seq < 0 || seq >= s->v_issued)
+        return fail(LQT_ERR_INVALID, "lqt_sim_wait_v_upto: copy " + std::to_string(seq) + " not issued (" +
+                                         std::to_string(s->v_issued) + " so far)");
+    // copies complete in order (each one's chunks join on copy stream 0);
+    // the ones older than the last kVDone were waited for at issue
+    if (seq >= s->v_issued - lqt_sim::kVDone) CK(cudaEventSynchronize(s->vdone[seq % lqt_sim::kVDone]));
     return LQT_OK;
 }
 

@@ -283,8 +283,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
     const Clock ck = *gd.clk;
     const float *__restrict__ V = gd.vg[cur];
     const float *__restrict__ Vp = gd.vg[cur ^ 1];
-    const float inv_dt = (float)(1.0 / gd.dt);
-    const float inv_mac = (float)(1.0 / (sg.nsub * gd.dt));
+    const float inv_dt = sg.inv_dt, inv_mac = sg.inv_mac;
     const int64_t nt = gd.ntissue;
     const int64_t ntiles = (nt + kTile - 1) / kTile;
     unsigned long long n_offer = 0, n_acc = 0;

@@ -49,6 +49,7 @@ struct SurGrid {
     float kappa;                    // multiplier of out_bound in the residual check
     float vstep_max;                // bound on the macro step's ionic V change (mV)
     int nsub;                       // plain steps per macro step
+    float inv_dt, inv_mac;          // 1 / dt and 1 / (nsub dt), rounded from FP64 on the host
     int use_net;                    // 0: coarse step without the network
 };
 cudaError_t launch_sur_grid(const GridDev<float> &gd, const SurGrid &sg, int cur, int dim, cudaStream_t st);

@@ -90,16 +90,26 @@ class Sim:
         """V into a caller buffer (float32 or float64, length n)."""
         N.check(N.lib().lqt_sim_get_v(self._h, _p(out), int(out.dtype == np.float64)), "lqt_sim_get_v")
 
-    def get_v_async(self, out: np.ndarray):
-        """Start copying V into `out` (pinned for overlap); complete after wait_v()."""
+    def get_v_async(self, out: np.ndarray) -> int:
+        """Start copying V into `out` (pinned for overlap).  Returns the
+        copy's number (0, 1, ... over this simulation's life): `out` is
+        complete after wait_v(number) or wait_v()."""
         L = N.lib()
         L.lqt_sim_get_v_async.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
         N.check(L.lqt_sim_get_v_async(self._h, _p(out), int(out.dtype == np.float64)), "lqt_sim_get_v_async")
+        self._v_issued = getattr(self, "_v_issued", 0) + 1
+        return self._v_issued - 1
 
-    def wait_v(self):
+    def wait_v(self, upto: int | None = None):
+        """Wait for every read-back copy in flight, or (upto) for copies
+        0..upto only."""
         L = N.lib()
-        L.lqt_sim_wait_v.argtypes = [C.c_void_p]
-        N.check(L.lqt_sim_wait_v(self._h), "lqt_sim_wait_v")
+        if upto is None:
+            L.lqt_sim_wait_v.argtypes = [C.c_void_p]
+            N.check(L.lqt_sim_wait_v(self._h), "lqt_sim_wait_v")
+        else:
+            L.lqt_sim_wait_v_upto.argtypes = [C.c_void_p, C.c_int64]
+            N.check(L.lqt_sim_wait_v_upto(self._h, int(upto)), "lqt_sim_wait_v_upto")
 
     def tissue_index(self) -> np.ndarray:
         out = np.zeros(self.n, np.int64)

@@ -191,9 +191,40 @@ def test_async_v_readback_matches_sync(lq):
     # double precision buffers too
     b64 = np.zeros(sim.n)
     sim.step(7)
-    sim.get_v_async(b64)
+    assert sim.get_v_async(b64) == 6
     sim.wait_v()
     np.testing.assert_array_equal(b64, sim.get_v(as_double=True))
+    # a copy not issued yet is refused
+    with pytest.raises(lq.LqtError):
+        sim.wait_v(7)
+
+
+@pytest.mark.gpu
+def test_async_v_readback_ring_waits_per_copy(lq):
+    """More copies than the 16 device slots and the 64 kept completion
+    events, with a host ring of 5 buffers: before a buffer is reused the host
+    waits for the copy that last filled it (lqt_sim_wait_v_upto), which then
+    holds the V of its step."""
+    import torch
+    sh = lq.geometry.sheet(50, 40, s1_cols=3)
+    sim = lq.Sim(sh.types, 0.15, precision=lq.MIXED, model="lqt1")
+    sim.set_protocol(bcl=1000.0, s1_mask=sh.s1_mask, s1_start=0.0, s1_duration=2.0, s1_strength=-52.0)
+    ring = 5
+    bufs = [torch.empty(sim.n, dtype=torch.float32, pin_memory=True).numpy() for _ in range(ring)]
+    ref, checked = [], 0
+    for i in range(90):
+        sim.step(3)
+        ref.append(sim.get_v())
+        if i >= ring:
+            sim.wait_v(i - ring)
+            np.testing.assert_array_equal(bufs[i % ring], ref[i - ring])
+            checked += 1
+        assert sim.get_v_async(bufs[i % ring]) == i
+    sim.wait_v(89)
+    for i in range(85, 90):
+        np.testing.assert_array_equal(bufs[i % ring], ref[i])
+    sim.wait_v(3)                       # long complete: returns at once
+    assert checked == 85
 
 
 def test_async_steps_match_synchronous_steps(lq):
@@ -224,11 +255,10 @@ def test_async_steps_match_synchronous_steps(lq):
     ref = []
     for i in range(K):
         a.step_async(1)
-        if i % ring == 0 and i > 0:
-            a.wait_v()
-            for j in range(ring):
-                np.testing.assert_array_equal(bufs[j], ref[i - ring + j])
-        a.get_v_async(bufs[i % ring])
+        if i >= ring:
+            a.wait_v(i - ring)          # the copy that last filled this buffer
+            np.testing.assert_array_equal(bufs[i % ring], ref[i - ring])
+        assert a.get_v_async(bufs[i % ring]) == i
         b.step(1)
         ref.append(b.get_v())
     a.sync()
