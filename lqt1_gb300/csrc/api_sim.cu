@@ -107,6 +107,10 @@ struct lqt_sim {
     cudaStream_t copy_stream[kCopyStreams] = {};
     cudaEvent_t gathered = nullptr, chunk_done[kCopyStreams] = {}, vdone[kVDone] = {};
     int64_t v_issued = 0;           // lqt_sim_get_v_async calls so far (the next copy's number)
+    // state transfer (lqt_sim_get_state / set_state): the AoS staging buffer
+    // (aos) and the tissue-order V, kept after the first use (no allocation
+    // or device-wide free per call)
+    void *vtmp = nullptr;
     // output sampling: tissue mask of the dense grid, lattice buffer
     uint8_t *tmask = nullptr;
     double *samp = nullptr;
@@ -975,9 +979,9 @@ int lqt_sim_get_state(lqt_sim *s, double *state_host)
     if (!s || !state_host) return fail(LQT_ERR_INVALID, "lqt_sim_get_state: NULL");
     const int64_t n = s->ntissue;
     if (!s->aos && s->mem.alloc((void **)&s->aos, n * 320)) return LQT_ERR_NOMEM;
-    // V: gather into a temporary SoA v slot (the last block of aos), then unpack
-    void *vtmp = nullptr;
-    if (s->mem.alloc(&vtmp, n * 8)) return LQT_ERR_NOMEM;
+    // V: gather into the state-transfer V buffer, then unpack
+    if (!s->vtmp && s->mem.alloc(&s->vtmp, n * 8)) return LQT_ERR_NOMEM;
+    void *vtmp = s->vtmp;
     const int32_t *gi = s->dim > 1 ? s->gidx : nullptr;
     cudaError_t e;
     if (s->fp64()) {
@@ -989,8 +993,6 @@ int lqt_sim_get_state(lqt_sim *s, double *state_host)
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(state_host, s->aos, n * 320, cudaMemcpyDeviceToHost, s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    cudaFree(vtmp);
-    s->mem.ptrs.erase(std::remove(s->mem.ptrs.begin(), s->mem.ptrs.end(), vtmp), s->mem.ptrs.end());
     if (e != cudaSuccess) return fail(LQT_ERR_CUDA, std::string("lqt_sim_get_state: ") + cudaGetErrorString(e));
     return LQT_OK;
 }
@@ -1000,8 +1002,8 @@ int lqt_sim_set_state(lqt_sim *s, const double *state_host)
     if (!s || !state_host) return fail(LQT_ERR_INVALID, "lqt_sim_set_state: NULL");
     const int64_t n = s->ntissue;
     if (!s->aos && s->mem.alloc((void **)&s->aos, n * 320)) return LQT_ERR_NOMEM;
-    void *vtmp = nullptr;
-    if (s->mem.alloc(&vtmp, n * 8)) return LQT_ERR_NOMEM;
+    if (!s->vtmp && s->mem.alloc(&s->vtmp, n * 8)) return LQT_ERR_NOMEM;
+    void *vtmp = s->vtmp;
     const int32_t *gi = s->dim > 1 ? s->gidx : nullptr;
     const size_t rsz = s->fp64() ? 8 : 4;
     cudaError_t e = cudaMemcpyAsync(s->aos, state_host, n * 320, cudaMemcpyHostToDevice, s->stream);
@@ -1019,8 +1021,6 @@ int lqt_sim_set_state(lqt_sim *s, const double *state_host)
     }
     // launch_ghost also advanced the device clock: restore it
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    cudaFree(vtmp);
-    s->mem.ptrs.erase(std::remove(s->mem.ptrs.begin(), s->mem.ptrs.end(), vtmp), s->mem.ptrs.end());
     if (e != cudaSuccess) return fail(LQT_ERR_CUDA, std::string("lqt_sim_set_state: ") + cudaGetErrorString(e));
     // a new state ends any macro step in progress: every voxel runs the plain
     // step until the next macro-step boundary

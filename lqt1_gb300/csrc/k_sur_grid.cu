@@ -78,6 +78,7 @@ constexpr uint32_t kOffBar = kOffNorm + 4 * kMlpIn * 4;             // per group
 constexpr uint32_t kSmemBytes = kOffBar + 8 * kGroups + 16;
 static_assert(kOffXH % 1024 == 0 && kXHBytes % 1024 == 0, "operand tiles 1 KB aligned");
 static_assert(kSmemBytes <= 227 * 1024, "shared memory");
+static_assert(kOffNorm % 16 == 0, "normalisation pairs read as float4");
 
 // Copy a row-major [R][K] BF16 matrix into the K-major core layout, times
 // `scale` (a power of two: exact in BF16).
@@ -247,7 +248,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
     uint8_t *xh = smem + kOffXH + grp * kXHBytes;
     const bool use_net = sg.use_net != 0;
 
-    for (int j = tid; j < 4 * kMlpIn; j += blockDim.x) nrm[j] = sg.norm[j];
+    // normalisation, rearranged once per CTA: (scale, -mean * scale) per
+    // input (one FMA per feature), the output scales, and kappa times the
+    // residual bounds
+    for (int j = tid; j < kMlpIn; j += blockDim.x) {
+        const float mu = sg.norm[j], sc = sg.norm[kMlpIn + j];
+        nrm[2 * j] = sc;
+        nrm[2 * j + 1] = -mu * sc;
+        nrm[2 * kMlpIn + j] = sg.norm[2 * kMlpIn + j];
+        nrm[3 * kMlpIn + j] = sg.kappa * sg.norm[3 * kMlpIn + j];
+    }
     if (use_net) {
         // hidden layers halved (see silu2_bf16); biases as an extra k-step
         stage_kmajor(smem + kOffW1, sg.w.w1t, kMlpHid, kMlpIn, 0.5f);
@@ -357,8 +367,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
 #pragma unroll
                     for (int i = 0; i < 4; ++i) {
                         const int a = j * 8 + 2 * i;
-                        __nv_bfloat162 h = __floats2bfloat162_rn((f[a] - nrm[a]) * nrm[kMlpIn + a],
-                                                                 (f[a + 1] - nrm[a + 1]) * nrm[kMlpIn + a + 1]);
+                        const float4 q = *reinterpret_cast<const float4 *>(nrm + 2 * a);
+                        __nv_bfloat162 h = __floats2bfloat162_rn(fmaf(f[a], q.x, q.y), fmaf(f[a + 1], q.z, q.w));
                         p[i] = *reinterpret_cast<uint32_t *>(&h);
                     }
                     *row[j] = make_uint4(p[0], p[1], p[2], p[3]);
@@ -435,7 +445,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
             conc_ptrs(c, cp);
             gate_ptrs(c, gp);
             const float *osc = nrm + 2 * kMlpIn;
-            const float *obd = nrm + 3 * kMlpIn;
+            const float *kbd = nrm + 3 * kMlpIn;     // kappa * bound
 #pragma unroll
             for (int cc = 0; cc < 48; cc += 16) {
                 float v[16];
@@ -446,7 +456,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_sur_grid(GridDev<float> gd, Sur
                         const int j = cc + i;
                         if (j < kMlpNState) {
                             const float z = v[i];
-                            if (!(fabsf(z) <= sg.kappa * obd[j])) why |= 1u;
+                            if (!(fabsf(z) <= kbd[j])) why |= 1u;
                             const float d = z * osc[j];
                             if (j == 0) c.v += d;
                             else if (j < 9) cadd(*cp[j - 1], d);
