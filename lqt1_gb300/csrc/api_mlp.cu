@@ -36,6 +36,7 @@ struct lqt_mlp {
     DevMem mem;
     float *P = nullptr, *G = nullptr, *M = nullptr, *V = nullptr;
     __nv_bfloat16 *Pb = nullptr;
+    __nv_bfloat16 *W2t = nullptr, *W3t = nullptr;   // transposed BF16 weights for the data gradients
     float *norm = nullptr;          // in_mean[48], in_scale[48], out_scale[48], out_bound[48]
     int *err = nullptr;
     double *loss = nullptr;
@@ -77,8 +78,9 @@ static int upload_params(lqt_mlp *m, const std::vector<float> &p)
     return LQT_OK;
 }
 
-// K slices of the weight-gradient GEMMs (K = batch): about 256 rows each.
-static int splitk_for(int64_t B) { return (int)std::min<int64_t>(128, std::max<int64_t>(1, B / 256)); }
+// K slices of the weight-gradient GEMMs (K = batch): 64 rows (one staging
+// chunk) each, at most 128 slices, so that the three GEMMs fill the SMs.
+static int splitk_for(int64_t B) { return (int)std::min<int64_t>(128, std::max<int64_t>(1, B / 64)); }
 
 static int ensure_ws(lqt_mlp *m, int64_t B)
 {
@@ -138,11 +140,13 @@ static int forward_backward(lqt_mlp *m, const __nv_bfloat16 *X, const float *T, 
     CK(launch_gemm_bf16(g, st));
     CK(cudaMemsetAsync(m->loss, 0, 8, st));
     CK(launch_mse_grad(m->Y, T, B, m->nvalid, m->dY, m->loss, st));
-    g = gemm(m->dY, kMlpOut, 0, W3, kMlpHid, 0, b, kMlpHid, kMlpOut);
+    // data gradients: W^T as N x K operands with K contiguous
+    CK(launch_transpose_w(W2, W3, m->W2t, m->W3t, st));
+    g = gemm(m->dY, kMlpOut, 0, m->W3t, kMlpOut, 1, b, kMlpHid, kMlpOut);
     g.epi = kEpiDact; g.Z = m->Z2; g.Cb = m->dZ2;
     g.err = m->err;
     CK(launch_gemm_bf16(g, st));
-    g = gemm(m->dZ2, kMlpHid, 0, W2, kMlpHid, 0, b, kMlpHid, kMlpHid);
+    g = gemm(m->dZ2, kMlpHid, 0, m->W2t, kMlpHid, 1, b, kMlpHid, kMlpHid);
     g.epi = kEpiDact; g.Z = m->Z1; g.Cb = m->dZ1;
     g.err = m->err;
     CK(launch_gemm_bf16(g, st));
@@ -176,6 +180,8 @@ int lqt_mlp_create(uint64_t seed, void *stream, lqt_mlp **out)
     int rc = m->mem.alloc((void **)&m->P, kNParam * 4) | m->mem.alloc((void **)&m->G, kNParam * 4) |
              m->mem.alloc((void **)&m->M, kNParam * 4) | m->mem.alloc((void **)&m->V, kNParam * 4) |
              m->mem.alloc((void **)&m->Pb, kNParam * 2) | m->mem.alloc((void **)&m->norm, 4 * kMlpIn * 4) |
+             m->mem.alloc((void **)&m->W2t, kMlpHid * kMlpHid * 2) |
+             m->mem.alloc((void **)&m->W3t, kMlpHid * kMlpOut * 2) |
              m->mem.alloc((void **)&m->err, 16) | m->mem.alloc((void **)&m->loss, 16);
     if (rc) {
         delete m;

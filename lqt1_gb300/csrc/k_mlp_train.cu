@@ -44,7 +44,10 @@ __host__ __device__ inline int splitk_chunk(int K, int ksplit)
 __global__ void k_splitk_reduce(const float *__restrict__ partial, int64_t mn, int slices, float *__restrict__ C)
 {
     for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < mn; o += (int64_t)gridDim.x * blockDim.x) {
+        // unrolled: the slices' loads are issued together, the additions
+        // stay in slice order
         float acc = 0.f;
+#pragma unroll 16
         for (int z = 0; z < slices; ++z) acc += partial[(int64_t)z * mn + o];
         C[o] += acc;
     }
@@ -161,23 +164,50 @@ __global__ void __launch_bounds__(128) k_gemm_tc(GemmArgs g)
 #pragma unroll
             for (int i = 0; i < 32; ++i) ep[tid * kEpPitch + i] = v[i];
             __syncthreads();
+            // a warp takes rows warp, warp + 4, ...: the loop is unrolled and
+            // the pointers restrict-qualified, so that its global loads (the
+            // bias once, Z of every row) are issued together instead of one
+            // latency per row behind the previous row's stores
             const int n = n0 + lane;
-            for (int r = warp; r < kTM; r += 4) {
-                const int m = m0 + r;
-                if (m >= g.M || n >= g.N) continue;
-                const int64_t o = (int64_t)m * g.N + n;
-                float x = ep[r * kEpPitch + lane];
-                if (g.epi == kEpiStore) {
-                    if (g.bias) x += g.bias[n];
-                    if (g.C) g.C[o] = x;
-                    if (g.Cb) g.Cb[o] = __float2bfloat16(g.act ? x * sigm(x) : x);
-                } else if (g.epi == kEpiDact) {
-                    const float z = g.Z[o], sz = sigm(z);
-                    g.Cb[o] = __float2bfloat16(x * (sz + z * sz * (1.0f - sz)));
-                } else if (slab) {
-                    slab[o] = x;
-                } else {
-                    atomicAdd(&g.C[o], x);
+            const bool nin = n < g.N;
+            const float *__restrict__ Zp = g.Z;
+            float *__restrict__ Cp = g.C;
+            __nv_bfloat16 *__restrict__ Cbp = g.Cb;
+            constexpr int kRows = kTM / 4;
+            if (g.epi == kEpiDact) {
+                float zv[kRows];
+#pragma unroll
+                for (int i = 0; i < kRows; ++i) {
+                    const int m = m0 + warp + 4 * i;
+                    zv[i] = (nin && m < g.M) ? Zp[(int64_t)m * g.N + n] : 0.f;
+                }
+#pragma unroll
+                for (int i = 0; i < kRows; ++i) {
+                    const int r = warp + 4 * i, m = m0 + r;
+                    if (!nin || m >= g.M) continue;
+                    const float x = ep[r * kEpPitch + lane], z = zv[i], sz = sigm(z);
+                    Cbp[(int64_t)m * g.N + n] = __float2bfloat16(x * (sz + z * sz * (1.0f - sz)));
+                }
+            } else if (g.epi == kEpiStore) {
+                const float bn = (nin && g.bias) ? g.bias[n] : 0.f;
+#pragma unroll 8
+                for (int i = 0; i < kRows; ++i) {
+                    const int r = warp + 4 * i, m = m0 + r;
+                    if (!nin || m >= g.M) continue;
+                    const int64_t o = (int64_t)m * g.N + n;
+                    const float x = ep[r * kEpPitch + lane] + bn;
+                    if (Cp) Cp[o] = x;
+                    if (Cbp) Cbp[o] = __float2bfloat16(g.act ? x * sigm(x) : x);
+                }
+            } else {
+#pragma unroll 8
+                for (int i = 0; i < kRows; ++i) {
+                    const int r = warp + 4 * i, m = m0 + r;
+                    if (!nin || m >= g.M) continue;
+                    const int64_t o = (int64_t)m * g.N + n;
+                    const float x = ep[r * kEpPitch + lane];
+                    if (slab) slab[o] = x;
+                    else atomicAdd(&Cp[o], x);
                 }
             }
             __syncthreads();
@@ -217,6 +247,24 @@ int gemm_splitk_slices(int K, int ksplit)
     if (ksplit <= 1 || K <= 0) return 0;
     const int chunk = splitk_chunk(K, ksplit);
     return (K + chunk - 1) / chunk;
+}
+
+// dst[c][r] = src[r][c] for the hidden and output weights (BF16): the
+// backward pass's data-gradient GEMMs read W as an N x K operand with K
+// contiguous, which the staging then copies with 16-byte loads.
+__global__ void k_transpose_w(const __nv_bfloat16 *__restrict__ w2, const __nv_bfloat16 *__restrict__ w3,
+                              __nv_bfloat16 *__restrict__ w2t, __nv_bfloat16 *__restrict__ w3t)
+{
+    const int n2 = kMlpHid * kMlpHid, n3 = kMlpOut * kMlpHid;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2 + n3; i += gridDim.x * blockDim.x) {
+        if (i < n2) {
+            const int r = i / kMlpHid, c = i - r * kMlpHid;
+            w2t[c * kMlpHid + r] = w2[i];
+        } else {
+            const int j = i - n2, r = j / kMlpHid, c = j - r * kMlpHid;
+            w3t[c * kMlpOut + r] = w3[j];
+        }
+    }
 }
 
 // ---- loss gradient and Adam -------------------------------------------------
@@ -290,6 +338,13 @@ cudaError_t launch_colsum(const __nv_bfloat16 *X, int64_t B, int N, float *g, cu
     k_colsum<<<N, 256, 0, st>>>(X, B, N, g);
     return cudaGetLastError();
 }
+cudaError_t launch_transpose_w(const __nv_bfloat16 *w2, const __nv_bfloat16 *w3, __nv_bfloat16 *w2t,
+                               __nv_bfloat16 *w3t, cudaStream_t st)
+{
+    k_transpose_w<<<(kMlpHid * (kMlpHid + kMlpOut) + 255) / 256, 256, 0, st>>>(w2, w3, w2t, w3t);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_adam(float *p, const float *g, float *m, float *v, __nv_bfloat16 *pb, int64_t n, float lr,
                         float b1, float b2, float eps, float c1, float c2, cudaStream_t st)
 {

@@ -55,5 +55,8 @@ struct GemmArgs {
 // Slices of a split-K GEMM and the workspace floats it needs (0 without a split).
 int gemm_splitk_slices(int K, int ksplit);
 cudaError_t launch_gemm_bf16(const GemmArgs &g, cudaStream_t st);
+// W2^T [in][out] and W3^T [in][out] from W2 [out][in], W3 [out][in] (BF16).
+cudaError_t launch_transpose_w(const __nv_bfloat16 *w2, const __nv_bfloat16 *w3, __nv_bfloat16 *w2t,
+                               __nv_bfloat16 *w3t, cudaStream_t st);
 
 }  // namespace lqt
