@@ -390,3 +390,47 @@ def test_substep_wait_timeout_is_reported_and_recoverable(lq, net, variant):
     assert sim.check() == 0
     assert np.isfinite(sim.get_state()).all()
     sim.close()
+
+
+def test_wave_foot_gate_on_a_premature_wave(lq, net):
+    """The S1-S2 sheet of the 2D workload at 200 x 200 (0.15 mm, LQT1 model,
+    S2 over a quadrant at the seeded coupling interval): the S2 wave runs into
+    recovering tissue with a long, slow foot.  Its activation time per voxel
+    (first upward crossing of -30 mV, V read back every step for 250 ms)
+    against the FP64 form: with the wave-foot gate (no macro step where V
+    below -40 mV rises faster than 0.1 mV/ms) the mean error is under 1.5 ms
+    and under half of the error without the gate (measured: 0.99 against
+    3.13 ms)."""
+    rng = np.random.default_rng(7)
+    ci = float(rng.uniform(300.0, 360.0))
+    m = lq.model("lqt1", gks_scale=0.5)
+    sh = lq.geometry.sheet(200, 200)
+
+    def s2_activation(prec, foot=None):
+        sim = lq.Sim(sh.types, 0.15, precision=prec, model=m, vmin_ok=-1e9, vmax_ok=1e9)
+        sim.set_protocol(bcl=1000.0, s1_mask=sh.s1_mask, s1_start=0.0, s1_duration=2.0, s1_strength=-52.0,
+                         s1_beats=1, s2_time=ci, s2_duration=3.0, s2_strength=-104.0, s2_mask=sh.s2_mask)
+        if foot is not None:
+            sim.set_surrogate(net, foot_dvdt=foot)
+        sim.step(int(round(ci / 0.02)))
+        vold = sim.get_v()
+        act = np.full(sim.n, -1.0)
+        for _ in range(int(round(250.0 / 0.02))):
+            t = sim.time
+            sim.step(1)
+            v = sim.get_v()
+            act[(vold < -30.0) & (v >= -30.0) & (act < 0)] = t
+            vold = v
+        assert sim.check() == 0
+        sim.close()
+        return act
+
+    ref = s2_activation(lq.FP64)
+    assert (ref >= 0).mean() > 0.99                # the S2 wave reaches the whole sheet
+
+    def mean_err(act):
+        both = (act >= 0) & (ref >= 0)
+        assert both.sum() > 0.99 * (ref >= 0).sum()
+        return float(np.abs(act - ref)[both].mean())
+    gated, ungated = mean_err(s2_activation(lq.MIXED, 0.1)), mean_err(s2_activation(lq.MIXED, 0.0))
+    assert gated < 1.5 and gated < 0.5 * ungated, (gated, ungated)

@@ -76,6 +76,8 @@ def test_surrogate_arguments_are_rejected_without_a_gpu(lq):
     assert lib.lqt_sim_surrogate_rejections(None, None) == lq._native.ERR_INVALID
     assert lib.lqt_sim_step_async(None, 1) == lq._native.ERR_INVALID
     assert lib.lqt_sim_sync(None) == lq._native.ERR_INVALID
+    lib.lqt_sim_wait_v_upto.argtypes = [C.c_void_p, C.c_int64]
+    assert lib.lqt_sim_wait_v_upto(None, 0) == lq._native.ERR_INVALID
 
 
 def _compare_maps(lq, orc, grid):
