@@ -46,7 +46,8 @@ struct lqt_sim {
     // device
     void *vg[2] = {nullptr, nullptr};
     void *gate = nullptr, *d6 = nullptr, *b3 = nullptr, *coeff = nullptr, *dcoeff = nullptr;
-    __half2 *d6h = nullptr, *b3h = nullptr;   // FP16 tensor copies for the surrogate substep (pad_tiles rows)
+    __half2 *t3h = nullptr;         // FP16 tensor rows for the surrogate substep (pad_tiles rows)
+    double d_fibre = 0, d_trans = 0;  // the anisotropic tensor's coefficients (2D/3D with fibres)
     int32_t *vbox_hdr = nullptr, *vli = nullptr;   // V-halo boxes of the 3D substep (k_sur_substep_vbox)
     double *conc = nullptr, *aos = nullptr;
     int32_t *gidx = nullptr, *bnd_dst = nullptr, *bnd_src = nullptr;
@@ -185,8 +186,9 @@ struct lqt_sim {
         g.plist = in_macro ? plist : nullptr;
         g.plist_n = in_macro ? (const int64_t *)plist_n : nullptr;
         g.serr = in_macro ? sur_err : nullptr;
-        g.d6h = in_macro ? d6h : nullptr;
-        g.b3h = in_macro ? b3h : nullptr;
+        g.t3h = in_macro ? t3h : nullptr;
+        g.sub_dtr = (float)d_trans;
+        g.sub_dsg = d_fibre >= d_trans ? 1.f : -1.f;
         g.vbox_hdr = in_macro ? vbox_hdr : nullptr;
         g.vli = in_macro ? vli : nullptr;
         g.sub_skip_copy = sub_skip_copy;
@@ -710,6 +712,8 @@ int lqt_sim_create(const lqt_sim_params *params, const lqt_geometry *geom, lqt_s
         return fail(LQT_ERR_CUDA, std::string("lqt_sim_create: ") + cudaGetErrorString(e));
     }
     if (dim > 1 && geom->fibre) {
+        s->d_fibre = geom->d_fibre;
+        s->d_trans = geom->d_trans;
         std::vector<float> d6, b3;
         build_tensor(nx, ny, nz, geom->dx, s->tm, geom->fibre, geom->d_fibre, geom->d_trans, d6, b3);
         rc = s->fp64() ? (upload_conv<double>(s, s->d6, d6) | upload_conv<double>(s, s->b3, b3))
@@ -1276,12 +1280,12 @@ int lqt_sim_set_surrogate(lqt_sim *s, lqt_mlp *m, const lqt_sur_config *cfg)
         CK(cudaMemsetAsync(s->sur_err, 0, sizeof(int), s->stream));
     }
     // the substep streams the tensor in FP16 (made once, padded to whole tiles)
-    if (s->d6 && !s->d6h) {
+    if (s->d6 && !s->t3h) {
         const int64_t np = pad_tiles(s->ntissue);
-        if (s->mem.alloc((void **)&s->d6h, np * 12) | s->mem.alloc((void **)&s->b3h, np * 8)) return LQT_ERR_NOMEM;
-        CK(cudaMemsetAsync(s->d6h, 0, np * 12, s->stream));
-        CK(cudaMemsetAsync(s->b3h, 0, np * 8, s->stream));
-        CK(launch_tensor_f16((const float *)s->d6, (const float *)s->b3, s->ntissue, s->d6h, s->b3h, s->stream));
+        if (s->mem.alloc((void **)&s->t3h, np * 12)) return LQT_ERR_NOMEM;
+        CK(cudaMemsetAsync(s->t3h, 0, np * 12, s->stream));
+        CK(launch_tensor_f16((const float *)s->d6, (const float *)s->b3, s->ntissue, (float)s->d_trans,
+                             s->d_fibre >= s->d_trans ? 1.f : -1.f, s->t3h, s->stream));
     }
     // the V-halo boxes of the 3D substep (whole z-segments: nz a multiple of 4)
     if (s->d6 && s->dim == 3 && s->nz % 4 == 0 && !s->vbox_hdr) {

@@ -61,10 +61,13 @@ template <typename R> struct GridDev {
     const int32_t *plist;
     const int64_t *plist_n;
     int *serr;                     // bit 1 set when a substep's copy wait ran out
-    // FP16 copies of the tensor (xx yy | zz xy | xz yz: 3 half2 per voxel) and
-    // of its divergence (x y | z 0: 2 half2 per voxel) that the surrogate's
-    // V-only substep streams; null without a surrogate or on isotropic grids
-    const __half2 *d6h, *b3h;
+    // the tensor rows that the surrogate's V-only substep streams, in FP16, 3
+    // half2 per voxel: (g_x g_y | g_z b_x | b_y b_z), with the tensor
+    // D = sub_dtr I + sub_dsg g g^T (g = sqrt|D_f - D_t| times the fibre
+    // direction, sub_dsg its sign) and b its divergence; null without a
+    // surrogate or on isotropic grids
+    const __half2 *t3h;
+    float sub_dtr, sub_dsg;
     // test of the failure path (lqt_sim_set_wait_test): 1 = the staged
     // substep leaves out the first tile's copies of every CTA, so that wait
     // runs out; wait_limit = polls per wait (0 = the default limit)

@@ -230,32 +230,30 @@ inline unsigned grid_list_blocks(int64_t ntissue)
 // read only where the macro-step kernel flagged that it can change.
 constexpr int kSubU = 2;
 
-// The surrogate substep's tensor rows in FP16 (3 half2 of the tensor, 2 of
-// the divergence per voxel; 2D reads the first 2 and 1): streaming loads,
-// widened to FP32 pairs.
-template <int DIM>
-__device__ __forceinline__ void sub_tensor_f16(const __half2 *d, const __half2 *b, float2 (&q)[5])
+// The surrogate substep's tensor row in FP16 (3 half2 per voxel: g_x g_y |
+// g_z b_x | b_y b_z, see GridDev::t3h): streaming loads, widened to FP32.
+__device__ __forceinline__ void sub_tensor_f16(const __half2 *t, float2 (&q)[3])
 {
 #pragma unroll
-    for (int i = 0; i < (DIM == 3 ? 3 : 2); ++i) q[i] = __half22float2(__ldcs(d + i));
-#pragma unroll
-    for (int i = 0; i < (DIM == 3 ? 2 : 1); ++i) q[3 + i] = __half22float2(__ldcs(b + i));
+    for (int i = 0; i < 3; ++i) q[i] = __half22float2(__ldcs(t + i));
 }
 
-template <int DIM> __device__ __forceinline__ void sub_tensor_unpack(const float2 (&q)[5], float *Dt, float *Bt)
+// The tensor (xx yy zz xy xz yz) and its divergence from a row:
+// D = dtr I + dsg g g^T.
+template <int DIM>
+__device__ __forceinline__ void sub_tensor_unpack(const float2 (&q)[3], float dtr, float dsg, float *Dt, float *Bt)
 {
-#pragma unroll
-    for (int i = 0; i < 6; ++i) Dt[i] = 0.f;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) Bt[i] = 0.f;
-#pragma unroll
-    for (int i = 0; i < (DIM == 3 ? 3 : 2); ++i) {
-        Dt[2 * i] = q[i].x;
-        Dt[2 * i + 1] = q[i].y;
-    }
-    Bt[0] = q[3].x;
-    Bt[1] = q[3].y;
-    if (DIM == 3) Bt[2] = q[4].x;
+    const float g0 = q[0].x, g1 = q[0].y, g2 = DIM == 3 ? q[1].x : 0.f;
+    const float s0 = dsg * g0, s1 = dsg * g1, s2 = dsg * g2;
+    Dt[0] = fmaf(s0, g0, dtr);
+    Dt[1] = fmaf(s1, g1, dtr);
+    Dt[2] = fmaf(s2, g2, dtr);
+    Dt[3] = s0 * g1;
+    Dt[4] = s0 * g2;
+    Dt[5] = s1 * g2;
+    Bt[0] = q[1].y;
+    Bt[1] = q[2].x;
+    Bt[2] = DIM == 3 ? q[2].y : 0.f;
 }
 
 // The anisotropic stencil of grid_du with the tensor already loaded, on any
@@ -296,7 +294,7 @@ template <int DIM, int MINB>
 __global__ void __launch_bounds__(256, MINB) k_sur_substep(GridDev<float> gd, float dt, int cur)
 {
     const int64_t k0 = blockIdx.x * (int64_t)(blockDim.x * kSubU) + threadIdx.x;
-    const bool aniso = DIM > 1 && gd.d6 && gd.d6h;
+    const bool aniso = DIM > 1 && gd.d6 && gd.t3h;
     float r[kSubU], Dt[kSubU][6], Bt[kSubU][3];
     int64_t g[kSubU];
     uint8_t ctl[kSubU], fl[kSubU];
@@ -316,9 +314,9 @@ __global__ void __launch_bounds__(256, MINB) k_sur_substep(GridDev<float> gd, fl
         if (aniso && on[u]) {
             // the FP16 copies, streamed once per step: evict-first, the L2 is
             // for the V rows
-            float2 q[5];
-            sub_tensor_f16<DIM>(gd.d6h + 3 * k, gd.b3h + 2 * k, q);
-            sub_tensor_unpack<DIM>(q, Dt[u], Bt[u]);
+            float2 q[3];
+            sub_tensor_f16(gd.t3h + 3 * k, q);
+            sub_tensor_unpack<DIM>(q, gd.sub_dtr, gd.sub_dsg, Dt[u], Bt[u]);
         }
     }
     bool any = false;

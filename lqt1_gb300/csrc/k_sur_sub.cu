@@ -15,19 +15,18 @@ namespace {
 constexpr uint32_t kSubWaitLimit = 1u << 22;   // bounded mbarrier polls per tile
 
 // One tile's rows, in the order of the copies: the macro step's ionic rate,
-// the dense index, the FP16 tensor (3 half2 per voxel), its FP16 divergence
-// (2 half2 per voxel), the control byte and the detector flag.
+// the dense index, the FP16 tensor row (3 half2 per voxel: the scaled fibre
+// direction and the divergence, GridDev::t3h), the control byte and the
+// detector flag.
 struct __align__(16) SubStage {
     float rate[kSubTile];
     int32_t gidx[kSubTile];
-    __half2 d6[kSubTile * 3];
-    __half2 b3[kSubTile * 2];
+    __half2 t3[kSubTile * 3];
     uint8_t ctl[kSubTile];
     uint8_t flag[kSubTile];
 };
-static_assert(sizeof(SubStage) % 16 == 0 && offsetof(SubStage, gidx) % 16 == 0 && offsetof(SubStage, d6) % 16 == 0 &&
-                  offsetof(SubStage, b3) % 16 == 0 && offsetof(SubStage, ctl) % 16 == 0 &&
-                  offsetof(SubStage, flag) % 16 == 0,
+static_assert(sizeof(SubStage) % 16 == 0 && offsetof(SubStage, gidx) % 16 == 0 && offsetof(SubStage, t3) % 16 == 0 &&
+                  offsetof(SubStage, ctl) % 16 == 0 && offsetof(SubStage, flag) % 16 == 0,
               "bulk copies need 16-byte aligned destinations");
 
 // Thread 0: the copies of tile k0 / kSubTile into one stage, completing on bar.
@@ -36,11 +35,10 @@ static_assert(sizeof(SubStage) % 16 == 0 && offsetof(SubStage, gidx) % 16 == 0 &
 __device__ __forceinline__ void sub_issue(SubStage &sg, uint64_t *bar, const GridDev<float> &gd, int64_t k0, bool det)
 {
     constexpr uint32_t n = kSubTile;
-    tc::mbar_expect_tx(bar, n * (4 + 4 + 12 + 8 + 1) + (det ? n : 0));
+    tc::mbar_expect_tx(bar, n * (4 + 4 + 12 + 1) + (det ? n : 0));
     tc::bulk_g2s(sg.rate, gd.srate + k0, n * 4, bar);
     tc::bulk_g2s(sg.gidx, gd.gidx + k0, n * 4, bar);
-    tc::bulk_g2s(sg.d6, gd.d6h + 3 * k0, n * 12, bar);
-    tc::bulk_g2s(sg.b3, gd.b3h + 2 * k0, n * 8, bar);
+    tc::bulk_g2s(sg.t3, gd.t3h + 3 * k0, n * 12, bar);
     tc::bulk_g2s(sg.ctl, gd.ctl + k0, n, bar);
     if (det) tc::bulk_g2s(sg.flag, gd.sdflag + k0, n, bar);
 }
@@ -100,13 +98,11 @@ __global__ void __launch_bounds__(kSubTile, MINB) k_sur_substep_tile(GridDev<flo
         const float r = sg.rate[t];
         if (k < gd.ntissue && r == r) {
             const int64_t g = sg.gidx[t];
-            float2 q[5];
+            float2 q[3];
 #pragma unroll
-            for (int i = 0; i < 3; ++i) q[i] = __half22float2(sg.d6[3 * t + i]);
-#pragma unroll
-            for (int i = 0; i < 2; ++i) q[3 + i] = __half22float2(sg.b3[2 * t + i]);
+            for (int i = 0; i < 3; ++i) q[i] = __half22float2(sg.t3[3 * t + i]);
             float Dt[6], Bt[3];
-            sub_tensor_unpack<DIM>(q, Dt, Bt);
+            sub_tensor_unpack<DIM>(q, gd.sub_dtr, gd.sub_dsg, Dt, Bt);
             const float vc = V[g];
             const float du = sub_du<DIM>(gd, V, g, k, vc, Dt, Bt);
             const float ist = grid_stim(gd, ck, sg.ctl[t], k);
@@ -157,9 +153,9 @@ __device__ __forceinline__ VHdr vhdr_load(const int32_t *h)
 
 // The producer warp's share of the copies of tile k0 / kSubTile into one
 // stage: lane 0 first writes the header and arms the stage's mbarrier with
-// the byte count, then the lanes issue the copies in parallel -- the 7 row
-// copies (rate, index, tensor, divergence, control, detector flag, box
-// index) and, when the box fits, one per box column.  A box column is the
+// the byte count, then the lanes issue the copies in parallel -- the 6 row
+// copies (rate, index, tensor row, control, detector flag, box index; 5
+// without the box) and, when the box fits, one per box column.  A box column is the
 // z-segment [zlo, zlo + bz) of grid column (xlo + i, ylo + j), copied whole:
 // nz, zlo and bz are multiples of 4, so every source and destination is
 // 16-byte aligned and every size a multiple of 16 bytes; the host builder
@@ -176,23 +172,22 @@ __device__ __forceinline__ void vbox_issue(typename StageOf<BOX>::T &st, uint64_
         st.hdr[1] = h.by * h.bz;
         st.hdr[2] = h.bz;
         const uint32_t box = (uint32_t)ncol * (uint32_t)h.bz * 4u;
-        tc::mbar_expect_tx(bar, n * (4 + 4 + 12 + 8 + 1) + (det ? n : 0) + (BOX ? n * 4 : 0) + box);
+        tc::mbar_expect_tx(bar, n * (4 + 4 + 12 + 1) + (det ? n : 0) + (BOX ? n * 4 : 0) + box);
     }
     __syncwarp();
-    for (int c = lane; c < (BOX ? 7 : 6) + ncol; c += 32) {
+    for (int c = lane; c < (BOX ? 6 : 5) + ncol; c += 32) {
         switch (c) {
         case 0: tc::bulk_g2s(st.rows.rate, gd.srate + k0, n * 4, bar); break;
         case 1: tc::bulk_g2s(st.rows.gidx, gd.gidx + k0, n * 4, bar); break;
-        case 2: tc::bulk_g2s(st.rows.d6, gd.d6h + 3 * k0, n * 12, bar); break;
-        case 3: tc::bulk_g2s(st.rows.b3, gd.b3h + 2 * k0, n * 8, bar); break;
-        case 4: tc::bulk_g2s(st.rows.ctl, gd.ctl + k0, n, bar); break;
-        case 5: if (det) tc::bulk_g2s(st.rows.flag, gd.sdflag + k0, n, bar); break;
+        case 2: tc::bulk_g2s(st.rows.t3, gd.t3h + 3 * k0, n * 12, bar); break;
+        case 3: tc::bulk_g2s(st.rows.ctl, gd.ctl + k0, n, bar); break;
+        case 4: if (det) tc::bulk_g2s(st.rows.flag, gd.sdflag + k0, n, bar); break;
         default:
             if constexpr (BOX) {
-                if (c == 6) {
+                if (c == 5) {
                     tc::bulk_g2s(st.li, gd.vli + k0, n * 4, bar);
                 } else {
-                    const int col = c - 7, i = col / h.by, j = col - i * h.by;
+                    const int col = c - 6, i = col / h.by, j = col - i * h.by;
                     tc::bulk_g2s(st.vb + col * h.bz, V + ((int64_t)(h.xlo + i) * ny + (h.ylo + j)) * nz + h.zlo,
                                  (uint32_t)h.bz * 4u, bar);
                 }
@@ -293,13 +288,11 @@ __global__ void __launch_bounds__(kSubTile + 32, MINB) k_sur_substep_vbox(GridDe
         const float r = sg.rate[t];
         if (k < gd.ntissue && r == r) {
             const int64_t g = sg.gidx[t];
-            float2 q[5];
+            float2 q[3];
 #pragma unroll
-            for (int i = 0; i < 3; ++i) q[i] = __half22float2(sg.d6[3 * t + i]);
-#pragma unroll
-            for (int i = 0; i < 2; ++i) q[3 + i] = __half22float2(sg.b3[2 * t + i]);
+            for (int i = 0; i < 3; ++i) q[i] = __half22float2(sg.t3[3 * t + i]);
             float Dt[6], Bt[3];
-            sub_tensor_unpack<DIM>(q, Dt, Bt);
+            sub_tensor_unpack<DIM>(q, gd.sub_dtr, gd.sub_dsg, Dt, Bt);
             float vc, du;
             bool staged = false;
             if constexpr (BOX) {
@@ -388,7 +381,7 @@ bool al16(const void *p) { return p && ((uintptr_t)p & 15u) == 0; }
 cudaError_t launch_sur_substep(const GridDev<float> &gd, double dt, int cur, int dim, int variant, cudaStream_t st)
 {
     if (gd.ntissue <= 0) return cudaSuccess;
-    const bool rows_ok = dim >= 2 && gd.d6 && al16(gd.d6h) && al16(gd.b3h) && al16(gd.srate) && al16(gd.gidx) &&
+    const bool rows_ok = dim >= 2 && gd.d6 && al16(gd.t3h) && al16(gd.srate) && al16(gd.gidx) &&
                          al16(gd.ctl) && gd.serr && (!gd.det || al16(gd.sdflag));
     if (variant >= 300) {
         // rows staged by a producer warp, V from the grid (2D/3D)
@@ -410,8 +403,8 @@ cudaError_t launch_sur_substep(const GridDev<float> &gd, double dt, int cur, int
     }
     const bool tile = variant >= 100;
     const int minb = tile ? variant - 100 : variant;
-    if (dim >= 2 && gd.d6 && !(gd.d6h && gd.b3h)) return cudaErrorInvalidValue;   // FP16 tensor copies missing
-    if (tile && dim >= 2 && gd.d6 && al16(gd.d6h) && al16(gd.b3h) && al16(gd.srate) && al16(gd.gidx) &&
+    if (dim >= 2 && gd.d6 && !gd.t3h) return cudaErrorInvalidValue;   // FP16 tensor rows missing
+    if (tile && dim >= 2 && gd.d6 && al16(gd.t3h) && al16(gd.srate) && al16(gd.gidx) &&
         al16(gd.ctl) && gd.serr && (!gd.det || al16(gd.sdflag))) {
         if (dim == 2) {
             if (minb == 8) return launch_tile<2, 8>(gd, dt, cur, st);

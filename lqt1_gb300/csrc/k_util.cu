@@ -132,24 +132,35 @@ cudaError_t launch_sample_v(const R *vg, const uint8_t *tissue, int32_t nx, int3
 }
 // FP16 copies of the FP32 tensor rows (6 per voxel) and divergence rows (3
 // per voxel, padded to 4) for the surrogate's substep.
-__global__ void k_tensor_f16(const float *__restrict__ d6, const float *__restrict__ b3, int64_t n,
-                             __half2 *__restrict__ d6h, __half2 *__restrict__ b3h)
+// The substep's FP16 tensor rows.  Every tensor is D = D_t I + dd f f^T
+// (xx yy zz xy xz yz in d6), so D - D_t I = sgn g g^T with g = sqrt|dd| f:
+// g is read off the largest diagonal entry of sgn (D - D_t I) (at least a
+// third of |dd| |f|^2) and the off-diagonal entries of its row.
+__global__ void k_tensor_f16(const float *__restrict__ d6, const float *__restrict__ b3, int64_t n, float dtr,
+                             float sgn, __half2 *__restrict__ t3h)
 {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
         const float *d = d6 + 6 * k, *b = b3 + 3 * k;
-        d6h[3 * k + 0] = __floats2half2_rn(d[0], d[1]);
-        d6h[3 * k + 1] = __floats2half2_rn(d[2], d[3]);
-        d6h[3 * k + 2] = __floats2half2_rn(d[4], d[5]);
-        b3h[2 * k + 0] = __floats2half2_rn(b[0], b[1]);
-        b3h[2 * k + 1] = __floats2half2_rn(b[2], 0.f);
+        const float a[3] = {sgn * (d[0] - dtr), sgn * (d[1] - dtr), sgn * (d[2] - dtr)};
+        const float off[3][3] = {{0.f, d[3], d[4]}, {d[3], 0.f, d[5]}, {d[4], d[5], 0.f}};
+        const int i = a[0] >= a[1] ? (a[0] >= a[2] ? 0 : 2) : (a[1] >= a[2] ? 1 : 2);
+        float g[3] = {0.f, 0.f, 0.f};
+        if (a[i] > 0.f) {
+            g[i] = sqrtf(a[i]);
+            for (int j = 0; j < 3; ++j)
+                if (j != i) g[j] = sgn * off[i][j] / g[i];
+        }
+        t3h[3 * k + 0] = __floats2half2_rn(g[0], g[1]);
+        t3h[3 * k + 1] = __floats2half2_rn(g[2], b[0]);
+        t3h[3 * k + 2] = __floats2half2_rn(b[1], b[2]);
     }
 }
 
-cudaError_t launch_tensor_f16(const float *d6, const float *b3, int64_t n, __half2 *d6h, __half2 *b3h,
+cudaError_t launch_tensor_f16(const float *d6, const float *b3, int64_t n, float dtr, float sgn, __half2 *t3h,
                               cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
-    k_tensor_f16<<<grid_for(n, 256), 256, 0, st>>>(d6, b3, n, d6h, b3h);
+    k_tensor_f16<<<grid_for(n, 256), 256, 0, st>>>(d6, b3, n, dtr, sgn, t3h);
     return cudaGetLastError();
 }
 

@@ -102,7 +102,9 @@ namespace lqt {
 template <typename R, typename T>
 cudaError_t launch_gather_v(const R *vg, const int32_t *gidx, T *out, int64_t n, cudaStream_t st);
 template <typename R> cudaError_t launch_scatter_v(const R *v, const int32_t *gidx, R *vg, int64_t n, cudaStream_t st);
-cudaError_t launch_tensor_f16(const float *d6, const float *b3, int64_t n, __half2 *d6h, __half2 *b3h,
+// FP16 tensor rows of the surrogate substep (grid_dev.h, GridDev::t3h) from
+// the FP32 tensor and divergence; dtr = D_t, sgn = the sign of D_f - D_t.
+cudaError_t launch_tensor_f16(const float *d6, const float *b3, int64_t n, float dtr, float sgn, __half2 *t3h,
                               cudaStream_t st);
 template <typename R>
 cudaError_t launch_sample_v(const R *vg, const uint8_t *tissue, int32_t nx, int32_t ny, int32_t nz, int32_t stride,
