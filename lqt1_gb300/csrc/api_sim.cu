@@ -51,6 +51,7 @@ struct lqt_sim {
     int32_t *vbox_hdr = nullptr, *vli = nullptr;   // V-halo boxes of the 3D substep (k_sur_substep_vbox)
     double *conc = nullptr, *aos = nullptr;
     int32_t *gidx = nullptr, *bnd_dst = nullptr, *bnd_src = nullptr;
+    float *xpos = nullptr;          // 2D/3D: (float)(i * dx), i < max(nx, ny, nz)
     uint8_t *ctl = nullptr;
     float *onset = nullptr;
     Clock *clk = nullptr;
@@ -155,6 +156,7 @@ struct lqt_sim {
         g.sy = dim == 2 ? 1 : nz;
         g.pad = 0;
         g.dx = dx;
+        g.xpos = xpos;
         g.inv_dx = (R)(1.0 / dx);
         g.inv_2dx = (R)(1.0 / (2.0 * dx));
         g.inv_dx2 = (R)(1.0 / (dx * dx));
@@ -711,7 +713,16 @@ int lqt_sim_create(const lqt_sim_params *params, const lqt_geometry *geom, lqt_s
         delete s;
         return fail(LQT_ERR_CUDA, std::string("lqt_sim_create: ") + cudaGetErrorString(e));
     }
-    if (dim > 1 && geom->fibre) {
+    if (!rc && dim > 1) {
+        const int32_t nmax = std::max(nx, std::max(ny, nz));
+        std::vector<float> xp(nmax);
+        for (int32_t i = 0; i < nmax; ++i) xp[i] = (float)(i * geom->dx);
+        if (s->mem.alloc((void **)&s->xpos, (size_t)nmax * 4)) rc = LQT_ERR_NOMEM;
+        else if (cudaMemcpyAsync(s->xpos, xp.data(), (size_t)nmax * 4, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+                 cudaStreamSynchronize(st) != cudaSuccess)
+            rc = fail(LQT_ERR_CUDA, "lqt_sim_create: coordinate table upload failed");
+    }
+    if (!rc && dim > 1 && geom->fibre) {
         s->d_fibre = geom->d_fibre;
         s->d_trans = geom->d_trans;
         std::vector<float> d6, b3;

@@ -37,6 +37,9 @@ template <typename R> struct GridDev {
     int64_t pad;                   // grid origin offset (0)
     double dx;
     R inv_dx, inv_2dx, inv_dx2, inv_4dx2;
+    // 2D/3D: (float)(i * dx) for i < max(nx, ny, nz), the voxel coordinates
+    // in mm that the pseudo-ECG uses (rounded once from FP64 on the host)
+    const float *xpos;
     double dt;
     ModelT<R> model;
     Clock *clk;

@@ -395,7 +395,7 @@ __global__ void __launch_bounds__(256) k_ecg_partial(GridDev<R> gd, const R *__r
                                                      const float4 *__restrict__ el, int nel,
                                                      double *__restrict__ partial)
 {
-    __shared__ double red[8][8];
+    __shared__ float2 red[8][kMaxElectrodes];
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     float acc[kMaxElectrodes];
 #pragma unroll
@@ -412,9 +412,12 @@ __global__ void __launch_bounds__(256) k_ecg_partial(GridDev<R> gd, const R *__r
             const int32_t g32 = (int32_t)g, sx32 = (int32_t)gd.sx, sy32 = (int32_t)gd.sy;
             const int32_t x = g32 / sx32, rem = g32 - x * sx32;
             const int32_t y = rem / sy32, z = rem - y * sy32;
-            p[0] = (float)((x - gd.pad) * gd.dx);
-            p[1] = (float)((y - gd.pad) * gd.dx);
-            p[2] = (float)((DIM == 3 ? z - gd.pad : 0) * gd.dx);
+            // coordinates from the host's table (no FP64 arithmetic per voxel:
+            // GB300's FP64 pipe would set this kernel's pace); the grid's
+            // origin offset is 0
+            p[0] = gd.xpos[x];
+            p[1] = gd.xpos[y];
+            p[2] = DIM == 3 ? gd.xpos[z] : 0.f;
             h[0] = 0.5f * (float)(V[g + gd.sx] - V[g - gd.sx]);
             h[1] = 0.5f * (float)(V[g + gd.sy] - V[g - gd.sy]);
             if constexpr (DIM == 3) h[2] = 0.5f * (float)(V[g + 1] - V[g - 1]);
@@ -440,13 +443,20 @@ __global__ void __launch_bounds__(256) k_ecg_partial(GridDev<R> gd, const R *__r
             kahan2_add(hi, lo, oh);
             lo = __fadd_rn(lo, ol);
         }
-        if (lane == 0) red[wid][e] = (double)hi + (double)lo;
+        if (lane == 0) red[wid][e] = make_float2(hi, lo);
     }
     __syncthreads();
+    // the block's warps, still as compensated FP32 pairs: one FP64 sum per
+    // electrode and block (a per-warp FP64 sum kept GB300's FP64 pipe busy
+    // for most of this kernel's time)
     if (threadIdx.x < nel) {
-        double s = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w][threadIdx.x];
-        partial[(int64_t)blockIdx.x * nel + threadIdx.x] = s;
+        float hi = 0.f, lo = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            const float2 v = red[w][threadIdx.x];
+            kahan2_add(hi, lo, v.x);
+            lo = __fadd_rn(lo, v.y);
+        }
+        partial[(int64_t)blockIdx.x * nel + threadIdx.x] = (double)hi + (double)lo;
     }
 }
 
