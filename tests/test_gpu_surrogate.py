@@ -313,7 +313,8 @@ def test_substep_variants_bit_identical(lq, net, dim):
 
 def test_macro_length_and_rejection_counters(lq, orc, net):
     """The macro length follows the network unless overridden (it must divide
-    the 50-step graph span); each residual check's failures are counted: with
+    the 50-step graph span) and bad wave-foot settings are refused; each
+    residual check's failures are counted: with
     a vanishing network bound every offered voxel fails it and none is
     accepted, and the voxels then take plain steps."""
     st = orc.initial_state(-87.5)
@@ -333,6 +334,10 @@ def test_macro_length_and_rejection_counters(lq, orc, net):
     for bad in (7, 51, -2):
         with pytest.raises(lq.LqtError):
             sim_with(nsub=bad)
+    # the wave-foot gate's rate bound must be >= 0 (0 = off) and its voltage finite
+    for bad in (dict(foot_dvdt=-0.1), dict(foot_v=float("nan")), dict(foot_v=float("inf"))):
+        with pytest.raises(lq.LqtError):
+            sim_with(**bad)
     sim = sim_with(nsub=5)
     sim.step(20)
     s5 = sim.surrogate_stats()
