@@ -326,7 +326,8 @@ int lqt_sim_set_electrodes(lqt_sim *s, int32_t n, const double *xyz_host,
  * copies V back every step, GPU3D.cu:1802): the gather into one of 16 device
  * slots runs on the simulation's stream, the copy on four copy streams, so it
  * overlaps the next steps; the steps wait only when all 16 slots hold copies
- * still in flight.  The copies of one simulation are numbered 0, 1, ... in
+ * still in flight.  The first call allocates the slots (16 x ntissue x 8
+ * bytes of device memory, kept until lqt_sim_destroy).  The copies of one simulation are numbered 0, 1, ... in
  * call order (the first call after lqt_sim_create is copy 0) and complete in
  * that order.  The buffer (pinned memory for a true overlap) is complete after
  * lqt_sim_wait_v_upto(its number) or lqt_sim_wait_v, and must not be reused
